@@ -1,0 +1,192 @@
+"""Seeded synthetic interferometer observations.
+
+No public dataset is available offline, so the imaging configurations are
+driven by synthetic visibilities with the shapes, layouts and value
+distributions of the workloads they stand in for:
+
+* antenna layouts in a local ENU frame (uniform disk or 3-arm log spiral);
+* Earth-rotation synthesis uvw: ENU -> local equatorial XYZ at latitude
+  ``lat`` (X = -sin(lat) N + cos(lat) U, Y = E, Z = cos(lat) N + sin(lat) U),
+  hour angle H = omega_E (t - t_mid), and the standard rotation to (u, v, w)
+  for declination ``dec``;
+* point-source skies, V(u,v) = sum_k S_k exp(-2 pi i (u l_k + v m_k) f/c)
+  (w ignored, as the gridder ignores it), plus complex Gaussian noise.
+
+Arrays use the visibility layout of the reference's vis datasets:
+DATA/WEIGHT/FLAG are (time, baseline, chan, pol) and UVW is
+(time, baseline, 3) in metres.
+"""
+import numpy as np
+
+C_LIGHT = 299792458.0
+OMEGA_EARTH = 7.2921e-5  # rad/s
+
+
+def disk_layout(n_ant, radius_m, rng):
+    """n_ant antennas uniform in a disk of the given radius (ENU metres)."""
+    r = radius_m * np.sqrt(rng.random(n_ant))
+    th = 2 * np.pi * rng.random(n_ant)
+    return np.stack([r * np.cos(th), r * np.sin(th), np.zeros(n_ant)], axis=1)
+
+
+def log_spiral_layout(n_ant, radius_m, rng, n_arms=3, r_min=20.0, turns=0.6):
+    """3-arm logarithmic spiral reaching ``radius_m``; small radial jitter."""
+    per_arm = int(np.ceil(n_ant / n_arms))
+    pos = []
+    for a in range(n_arms):
+        k = np.arange(per_arm)
+        r = r_min * (radius_m / r_min) ** (k / max(per_arm - 1, 1))
+        th = 2 * np.pi * a / n_arms + 2 * np.pi * turns * np.log(r / r_min) / np.log(radius_m / r_min)
+        r = r * (1 + 0.02 * rng.standard_normal(per_arm))
+        pos.append(np.stack([r * np.cos(th), r * np.sin(th), np.zeros(per_arm)], axis=1))
+    return np.concatenate(pos)[:n_ant]
+
+
+def baseline_pairs(n_ant):
+    a1, a2 = np.triu_indices(n_ant, k=1)
+    return a1.astype(np.int32), a2.astype(np.int32)
+
+
+def earth_rotation_uvw(enu, n_time, dt_s, lat_deg=34.0, dec_deg=45.0):
+    """uvw (T, B, 3) float64 in metres for all antenna pairs i<j."""
+    lat = np.deg2rad(lat_deg)
+    dec = np.deg2rad(dec_deg)
+    e, n, u = enu[:, 0], enu[:, 1], enu[:, 2]
+    X = -np.sin(lat) * n + np.cos(lat) * u
+    Y = e
+    Z = np.cos(lat) * n + np.sin(lat) * u
+    a1, a2 = baseline_pairs(len(enu))
+    bx, by, bz = X[a2] - X[a1], Y[a2] - Y[a1], Z[a2] - Z[a1]
+    t = (np.arange(n_time) - (n_time - 1) / 2.0) * dt_s
+    H = OMEGA_EARTH * t
+    sH, cH = np.sin(H)[:, None], np.cos(H)[:, None]
+    uu = sH * bx + cH * by
+    vv = -np.sin(dec) * cH * bx + np.sin(dec) * sH * by + np.cos(dec) * bz
+    ww = np.cos(dec) * cH * bx - np.cos(dec) * sH * by + np.sin(dec) * bz
+    return np.stack([uu, vv, ww], axis=-1).astype(np.float64)
+
+
+def pixel_to_lm(px, py, image_size, cell_rad):
+    """Direction cosines of image pixel (px, py) for this gridder's geometry.
+
+    With the cell_size[0] sign flip, a source at (l, m) = ((px - N0/2) c0,
+    -(py - N1/2) c1) peaks at pixel (px, py) of the dirty image.
+    """
+    l = (np.asarray(px) - image_size[0] // 2) * cell_rad[0]
+    m = -(np.asarray(py) - image_size[1] // 2) * cell_rad[1]
+    return l, m
+
+
+def point_source_vis(uvw, freq, l, m, flux, n_pol=2, noise_sigma=0.0, rng=None,
+                     device=None, dtype=np.complex64):
+    """Visibilities (T,B,C,P) of point sources; optional complex noise.
+
+    Runs in numpy, or with torch on ``device`` for large cubes (generation is
+    input preparation, not part of any timed region).
+    """
+    T, B = uvw.shape[:2]
+    C = len(freq)
+    if device is None:
+        out = np.zeros((T, B, C), dtype=np.complex128)
+        for c in range(C):
+            k = 2 * np.pi * freq[c] / C_LIGHT
+            acc = np.zeros((T, B), dtype=np.complex128)
+            for s in range(len(flux)):
+                ph = -k * (uvw[..., 0] * l[s] + uvw[..., 1] * m[s])
+                acc += flux[s] * np.exp(1j * ph)
+            out[..., c] = acc
+        vis = np.repeat(out[..., None], n_pol, axis=-1).astype(dtype)
+        if noise_sigma > 0:
+            rng = rng or np.random.default_rng(0)
+            vis = vis + (noise_sigma * (rng.standard_normal(vis.shape) + 1j * rng.standard_normal(vis.shape))).astype(dtype)
+        return vis
+    import torch
+    dev = torch.device(device)
+    u = torch.as_tensor(uvw[..., 0], device=dev, dtype=torch.float64)
+    v = torch.as_tensor(uvw[..., 1], device=dev, dtype=torch.float64)
+    lt = torch.as_tensor(np.asarray(l), device=dev, dtype=torch.float64)
+    mt = torch.as_tensor(np.asarray(m), device=dev, dtype=torch.float64)
+    st = torch.as_tensor(np.asarray(flux), device=dev, dtype=torch.float64)
+    vis = torch.empty((T, B, C, n_pol), dtype=torch.complex64, device=dev)
+    gen = torch.Generator(device=dev)
+    gen.manual_seed(int(rng.integers(1 << 31)) if rng is not None else 0)
+    for c in range(C):
+        k = 2 * np.pi * float(freq[c]) / C_LIGHT
+        re = torch.zeros((T, B), dtype=torch.float64, device=dev)
+        im = torch.zeros((T, B), dtype=torch.float64, device=dev)
+        for s0 in range(0, len(flux), 16):
+            ph = -k * (u[..., None] * lt[s0:s0 + 16] + v[..., None] * mt[s0:s0 + 16])
+            re += (st[s0:s0 + 16] * torch.cos(ph)).sum(-1)
+            im += (st[s0:s0 + 16] * torch.sin(ph)).sum(-1)
+        base = torch.complex(re.float(), im.float())
+        for p in range(n_pol):
+            vc = base
+            if noise_sigma > 0:
+                nr = torch.randn((T, B), generator=gen, device=dev) * noise_sigma
+                ni = torch.randn((T, B), generator=gen, device=dev) * noise_sigma
+                vc = vc + torch.complex(nr, ni)
+            vis[:, :, c, p] = vc
+    return vis
+
+
+class Observation(dict):
+    """Plain container for a synthetic observation (arrays + imaging parms)."""
+    __getattr__ = dict.__getitem__
+
+
+def make_observation(n_ant, layout, radius_m, n_time, dt_s, freq, n_pol, n_src,
+                     flux_range, src_radius_rad, noise_sigma, image_size, cell_arcsec,
+                     seed, flag_fraction=0.0, flux_law='uniform', vis_device=None,
+                     with_vis=True):
+    rng = np.random.default_rng(seed)
+    enu = disk_layout(n_ant, radius_m, rng) if layout == 'disk' else log_spiral_layout(n_ant, radius_m, rng)
+    uvw = earth_rotation_uvw(enu, n_time, dt_s)
+    T, B = uvw.shape[:2]
+    C = len(freq)
+    if flux_law == 'uniform':
+        flux = rng.uniform(flux_range[0], flux_range[1], n_src)
+    else:  # N(>S) ~ S^-1.5 between the bounds, inverse-CDF sampling
+        a, b = flux_range
+        x = rng.random(n_src)
+        flux = (a ** -1.5 - x * (a ** -1.5 - b ** -1.5)) ** (-1 / 1.5)
+    r = src_radius_rad * np.sqrt(rng.random(n_src))
+    th = 2 * np.pi * rng.random(n_src)
+    l, m = r * np.cos(th), r * np.sin(th)
+    obs = Observation(uvw=uvw, freq=np.asarray(freq, dtype=np.float64), l=l, m=m, flux=flux,
+                      enu=enu, image_size=list(image_size), cell_arcsec=list(cell_arcsec))
+    weight = np.ones((T, B, C, n_pol), dtype=np.float32)
+    flag = None
+    if flag_fraction > 0:
+        flag = rng.random((T, B, C, n_pol)) < flag_fraction
+    obs['weight'] = weight
+    obs['flag'] = flag
+    if with_vis:
+        vis = point_source_vis(uvw, obs['freq'], l, m, flux, n_pol, noise_sigma, rng, device=vis_device)
+        if flag is not None:
+            if vis_device is None:
+                vis[flag] = np.nan
+            else:
+                import torch
+                vis[torch.as_tensor(flag, device=vis.device)] = complex('nan')
+        obs['vis'] = vis
+    return obs
+
+
+def config_standard_small(seed=1, n_time=600, n_chan=32):
+    """Plain standard gridding workload: 27 antennas in a 1 km-radius disk,
+    600 x 10 s integrations, 32 channels 1.000-1.128 GHz (4 MHz), RR/LL,
+    20 sources, 512^2 image at 2 arcsec, natural weighting."""
+    freq = 1.000e9 + (np.arange(n_chan) + 0.5) * 4e6
+    return make_observation(27, 'disk', 1000.0, n_time, 10.0, freq, 2, 20, (0.1, 1.0),
+                            np.deg2rad(0.5), 0.1, (512, 512), (2.0, 2.0), seed)
+
+
+def config_large_cube(seed=2, n_time=1024, n_chan=256, vis_device=None, with_vis=True):
+    """Large cube: 64 antennas, 3-arm log spiral of 2.5 km radius, 1024 x 8 s,
+    256 channels over 1.0-1.5 GHz, RR/LL, 200 power-law sources
+    (1 mJy-1 Jy), 5% random flags, Briggs 0.5, 4096^2 image at 1 arcsec."""
+    freq = 1.0e9 + (np.arange(n_chan) + 0.5) * (0.5e9 / n_chan)
+    fov = 4096 * np.deg2rad(1.0 / 3600) / 2
+    return make_observation(64, 'log_spiral', 2500.0, n_time, 8.0, freq, 2, 200, (1e-3, 1.0),
+                            fov, 0.05, (4096, 4096), (1.0, 1.0), seed, flag_fraction=0.05,
+                            flux_law='power', vis_device=vis_device, with_vis=with_vis)

@@ -1,0 +1,176 @@
+// Inverse FFT of gridded planes, centre crop and gridding correction.
+//
+// Reference behaviour (make_image.py:116-130, make_psf.py:117-131,
+// _remove_padding.py:20-31):
+//     img = fftshift(ifft2(ifftshift(grid))) ; crop centre (n_l, n_m) window
+//     img = img.real * Nu*Nv / sum_weight(0->1) / correction
+// Because the gridder already wrote each plane in ifftshift order
+// (NGG_LAYOUT_FFT), the shifts reduce to index arithmetic: an unnormalised
+// inverse C2C transform (cuFFT, in place) followed by one epilogue kernel that
+// reads only the cropped window, applies the fftshift mapping
+// out[(l - n_l/2) mod Nu, (m - n_m/2) mod Nv], and divides by sum_weight and
+// the correction image. numpy's ifft2 times Nu*Nv equals cuFFT's unnormalised
+// CUFFT_INVERSE, so no scaling is applied.
+#include <cufft.h>
+
+#include <map>
+#include <mutex>
+#include <tuple>
+
+#include "ngg_internal.cuh"
+
+namespace ngg {
+
+namespace {
+struct PlanKey {
+    int dev;
+    int64_t nu, nv;
+    int batch;
+    bool operator<(const PlanKey &o) const {
+        return std::tie(dev, nu, nv, batch) < std::tie(o.dev, o.nu, o.nv, o.batch);
+    }
+};
+std::mutex g_plan_mu;
+std::map<PlanKey, cufftHandle> g_plans;
+
+int get_plan(int64_t nu, int64_t nv, int batch, cufftHandle *out) {
+    int dev = 0;
+    cudaGetDevice(&dev);
+    PlanKey k{dev, nu, nv, batch};
+    std::lock_guard<std::mutex> lk(g_plan_mu);
+    auto it = g_plans.find(k);
+    if (it != g_plans.end()) {
+        *out = it->second;
+        return NGG_OK;
+    }
+    cufftHandle h;
+    if (cufftCreate(&h) != CUFFT_SUCCESS) return fail(NGG_ERR_CUDA, "cufftCreate");
+    long long n[2] = {(long long)nu, (long long)nv};
+    size_t ws = 0;
+    cufftResult r = cufftMakePlanMany64(h, 2, n, nullptr, 1, nu * nv, nullptr, 1, nu * nv, CUFFT_C2C, batch, &ws);
+    if (r != CUFFT_SUCCESS) {
+        cufftDestroy(h);
+        return fail(r == CUFFT_ALLOC_FAILED ? NGG_ERR_NOMEM : NGG_ERR_CUDA, "cufftMakePlanMany64 failed");
+    }
+    g_plans[k] = h;
+    *out = h;
+    return NGG_OK;
+}
+
+// one thread per output pixel (l, m) of one plane batch
+__global__ void k_crop_correct(const float2 *planes, int nplanes, int plane0, int64_t nu, int64_t nv, int64_t nl,
+                               int64_t nm, int64_t n_planes_total, const double *sum_weight,
+                               const double *correction, double *image) {
+    const int64_t id = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (id >= nl * nm) return;
+    const int64_t l = id / nm, m = id % nm;
+    int64_t k1 = l - nl / 2, k2 = m - nm / 2;
+    if (k1 < 0) k1 += nu;
+    if (k2 < 0) k2 += nv;
+    const double corr = correction[id];
+    for (int q = 0; q < nplanes; ++q) {
+        const int64_t pl = plane0 + q;
+        double sw = sum_weight[pl];
+        if (sw == 0.0) sw = 1.0;
+        const float re = planes[(int64_t)q * nu * nv + k1 * nv + k2].x;
+        image[id * n_planes_total + pl] = ((double)re / sw) / corr;
+    }
+}
+// adjoint of k_crop_correct: scaled image values placed into zeroed planes
+__global__ void k_embed(const void *image, int is_f64, int nplanes, int plane0, int64_t nu, int64_t nv, int64_t nl,
+                        int64_t nm, int64_t n_planes_total, const double *sum_weight, const double *correction,
+                        float2 *planes) {
+    const int64_t id = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (id >= nl * nm) return;
+    const int64_t l = id / nm, m = id % nm;
+    int64_t k1 = l - nl / 2, k2 = m - nm / 2;
+    if (k1 < 0) k1 += nu;
+    if (k2 < 0) k2 += nv;
+    const double corr = correction[id];
+    for (int q = 0; q < nplanes; ++q) {
+        const int64_t pl = plane0 + q;
+        double sw = sum_weight[pl];
+        if (sw == 0.0) sw = 1.0;
+        const int64_t ii = id * n_planes_total + pl;
+        const double x = is_f64 ? ((const double *)image)[ii] : (double)((const float *)image)[ii];
+        planes[(int64_t)q * nu * nv + k1 * nv + k2] = make_float2((float)((x / sw) / corr), 0.f);
+    }
+}
+}  // namespace
+
+void release_fft_plans() {
+    std::lock_guard<std::mutex> lk(g_plan_mu);
+    for (auto &kv : g_plans) cufftDestroy(kv.second);
+    g_plans.clear();
+}
+
+}  // namespace ngg
+
+using namespace ngg;
+
+extern "C" int ngg_fft_correct(void *grid, int64_t n_img, int64_t P, int64_t nu, int64_t nv, int64_t nl, int64_t nm,
+                               const double *sum_weight, const double *correction, double *image, void *stream) {
+    clear_error();
+    cudaStream_t s = (cudaStream_t)stream;
+    if (n_img < 0 || P < 1 || nu < 1 || nv < 1 || nl < 1 || nm < 1 || nl > nu || nm > nv)
+        return fail(NGG_ERR_INVALID, "dims (need 1 <= n_l <= n_u, 1 <= n_m <= n_v)");
+    if (!grid || !sum_weight || !correction || !image) return fail(NGG_ERR_INVALID, "NULL pointer");
+    const int64_t n_planes = n_img * P;
+    if (n_planes == 0) return NGG_OK;
+    // batch size: bound the per-call working set to ~4 GB of planes
+    const int64_t plane_bytes = nu * nv * 8;
+    int64_t batch = (4ll << 30) / plane_bytes;
+    if (batch < 1) batch = 1;
+    if (batch > n_planes) batch = n_planes;
+    if (batch > 64) batch = 64;
+    float2 *g = (float2 *)grid;
+    for (int64_t p0 = 0; p0 < n_planes; p0 += batch) {
+        const int nb = (int)((n_planes - p0) < batch ? (n_planes - p0) : batch);
+        cufftHandle h;
+        int rc = get_plan(nu, nv, nb, &h);
+        if (rc != NGG_OK) return rc;
+        if (cufftSetStream(h, s) != CUFFT_SUCCESS) return fail(NGG_ERR_CUDA, "cufftSetStream");
+        float2 *base = g + p0 * nu * nv;
+        if (cufftExecC2C(h, (cufftComplex *)base, (cufftComplex *)base, CUFFT_INVERSE) != CUFFT_SUCCESS)
+            return fail(NGG_ERR_CUDA, "cufftExecC2C");
+        const int64_t npx = nl * nm;
+        k_crop_correct<<<(unsigned)((npx + 255) / 256), 256, 0, s>>>(base, nb, (int)p0, nu, nv, nl, nm, n_planes,
+                                                                     sum_weight, correction, image);
+        NGG_CHECK_LAUNCH("k_crop_correct");
+    }
+    return NGG_OK;
+}
+
+extern "C" int ngg_fft_correct_adjoint(const void *image, int is_f64, int64_t n_img, int64_t P, int64_t nu, int64_t nv,
+                                       int64_t nl, int64_t nm, const double *sum_weight, const double *correction,
+                                       void *grid, void *stream) {
+    clear_error();
+    cudaStream_t s = (cudaStream_t)stream;
+    if (n_img < 0 || P < 1 || nu < 1 || nv < 1 || nl < 1 || nm < 1 || nl > nu || nm > nv)
+        return fail(NGG_ERR_INVALID, "dims (need 1 <= n_l <= n_u, 1 <= n_m <= n_v)");
+    if (!grid || !sum_weight || !correction || !image) return fail(NGG_ERR_INVALID, "NULL pointer");
+    const int64_t n_planes = n_img * P;
+    if (n_planes == 0) return NGG_OK;
+    NGG_CUDA(cudaMemsetAsync(grid, 0, sizeof(float2) * n_planes * nu * nv, s));
+    const int64_t plane_bytes = nu * nv * 8;
+    int64_t batch = (4ll << 30) / plane_bytes;
+    if (batch < 1) batch = 1;
+    if (batch > n_planes) batch = n_planes;
+    if (batch > 64) batch = 64;
+    float2 *g = (float2 *)grid;
+    for (int64_t p0 = 0; p0 < n_planes; p0 += batch) {
+        const int nb = (int)((n_planes - p0) < batch ? (n_planes - p0) : batch);
+        float2 *base = g + p0 * nu * nv;
+        const int64_t npx = nl * nm;
+        k_embed<<<(unsigned)((npx + 255) / 256), 256, 0, s>>>(image, is_f64, nb, (int)p0, nu, nv, nl, nm, n_planes,
+                                                              sum_weight, correction, base);
+        NGG_CHECK_LAUNCH("k_embed");
+        cufftHandle h;
+        int rc = get_plan(nu, nv, nb, &h);
+        if (rc != NGG_OK) return rc;
+        if (cufftSetStream(h, s) != CUFFT_SUCCESS) return fail(NGG_ERR_CUDA, "cufftSetStream");
+        if (cufftExecC2C(h, (cufftComplex *)base, (cufftComplex *)base, CUFFT_FORWARD) != CUFFT_SUCCESS)
+            return fail(NGG_ERR_CUDA, "cufftExecC2C");
+    }
+    return NGG_OK;
+}

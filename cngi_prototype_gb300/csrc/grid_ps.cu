@@ -1,0 +1,819 @@
+// Standard (prolate-spheroidal) convolutional gridder for sm_103a.
+//
+// Reference behaviour: _standard_grid_jit
+// (ngcasa/imaging/_imaging_utils/_standard_grid.py:242-371) -- every
+// visibility whose 7x7 footprint lies inside the grid adds
+// conv_u*conv_v*weighted_datum to 49 cells and weight*sum(conv) to
+// sum_weight.
+//
+// GB300 design (one call = the whole cube):
+//  1. k_chan / k_uvw: per-channel uv scale (FP64, reference operation order)
+//     split into FP32 pairs; per (baseline, time) uvw split into FP32 pairs in
+//     baseline-major order; per 32-step track chunk a uv bounding box.
+//  2. Binning: every chunk (chan, baseline, 32 time steps) is listed in each
+//     64x64 uv-tile its footprint bounding box touches; keys
+//     (bin = (image chan, tile), chunk) are radix-sorted so every bin holds
+//     its chunks in (chan, baseline, time) order -- consecutive entries
+//     continue the same track.
+//  3. k_tiles: a persistent kernel; each CTA takes work items (tile, image
+//     channel) from a global counter, channel-fastest so CTAs working on
+//     neighbouring channels share the visibility lines in L2. Empty tiles
+//     are written as zeros; busy tiles are accumulated in shared memory and
+//     written once, coalesced. The grid is therefore written exactly once
+//     and never read back.
+//  Inside a busy tile each warp runs 8 track processors of 4 lanes. A lane
+//  owns up to two of the 7 column residue classes (Romein's work
+//  distribution) and, for each, the 7 rows of the current footprint in
+//  registers; it adds tap*tap*datum in registers while its cells stay the
+//  same and flushes a cell to shared memory (atomic add) only when the track
+//  moves off it. Taps come from the oversampled table, loaded into shared
+//  memory by a TMA bulk copy. Cell and oversampling indices are certified to
+//  equal the reference's FP64 results (see cell_pair).
+#include <cub/cub.cuh>
+
+#include <algorithm>
+#include <vector>
+
+#include "ngg_internal.cuh"
+
+namespace ngg {
+namespace {
+
+constexpr int TU = 64;      // tile rows (u)
+constexpr int TV = 64;      // tile columns (v, contiguous)
+constexpr int CH = 32;      // time steps per chunk
+constexpr int NW = 8;       // warps per CTA
+constexpr int NG = 8;       // track processors per warp (4 lanes each)
+constexpr int ROUND = 16;   // producer round length (steps)
+constexpr int SUP = 7;
+constexpr int SC = 3;
+constexpr int MAX_TAB = 4096;
+
+struct ChanParms {
+    double su, sv;
+    float suh, sul, svh, svl;
+};
+
+struct TileArgs {
+    const float2 *vis;        // (T,B,C,P)
+    const float *weight;      // (T,B,C,P)
+    const double *uvw;        // (T,B,3) (FP64 fallback only)
+    const float4 *uvs;        // [B][T] (u_hi,u_lo,v_hi,v_lo)
+    const ChanParms *chan;    // [C]
+    const float *tab_g;       // table (float), padded to 16 bytes
+    const unsigned long long *keys;
+    const int64_t *bin_start; // [n_bins + 1]
+    void *grid;
+    double *sum_weight;
+    int *work_counter;
+    int64_t T, B, C, P;
+    int64_t nu, nv;
+    int n_img, ntu, ntv, nk;
+    int p0;            // first pol of this launch
+    int os;
+    int tab_len;       // floats in the table
+    int tab_bytes;     // padded to 16
+    int continuum;
+};
+
+__global__ void k_chan(const double *freq, int C, double dl0, double dl1, int64_t nu, int64_t nv,
+                       ChanParms *out) {
+    int c = blockIdx.x * blockDim.x + threadIdx.x;
+    if (c >= C) return;
+    double su, sv;
+    uv_scale_dev(freq[c], dl0, dl1, nu, nv, su, sv);
+    ChanParms p;
+    p.su = su;
+    p.sv = sv;
+    Split a = split_double(su), b = split_double(sv);
+    p.suh = a.hi; p.sul = a.lo; p.svh = b.hi; p.svl = b.lo;
+    out[c] = p;
+}
+
+// one warp per (baseline, chunk): split uvw rows and reduce the chunk bbox
+__global__ void k_uvw(const double *uvw, int64_t T, int64_t B, int nk, float4 *uvs, float4 *bbox) {
+    int64_t w = (int64_t)blockIdx.x * (blockDim.x / 32) + threadIdx.x / 32;
+    int lane = threadIdx.x & 31;
+    if (w >= B * nk) return;
+    int64_t b = w / nk;
+    int k = (int)(w % nk);
+    int64_t t = (int64_t)k * CH + lane;
+    float umin = INFINITY, umax = -INFINITY, vmin = INFINITY, vmax = -INFINITY;
+    if (t < T) {
+        double u = uvw[(t * B + b) * 3 + 0];
+        double v = uvw[(t * B + b) * 3 + 1];
+        Split su = split_double(u), sv = split_double(v);
+        uvs[b * T + t] = make_float4(su.hi, su.lo, sv.hi, sv.lo);
+        if (!isnan(u) && !isnan(v)) {
+            umin = umax = su.hi;
+            vmin = vmax = sv.hi;
+        }
+    }
+    for (int o = 16; o > 0; o >>= 1) {
+        umin = fminf(umin, __shfl_xor_sync(0xffffffffu, umin, o));
+        umax = fmaxf(umax, __shfl_xor_sync(0xffffffffu, umax, o));
+        vmin = fminf(vmin, __shfl_xor_sync(0xffffffffu, vmin, o));
+        vmax = fmaxf(vmax, __shfl_xor_sync(0xffffffffu, vmax, o));
+    }
+    if (lane == 0) bbox[w] = make_float4(umin, umax, vmin, vmax);
+}
+
+struct TileRange { int u0, u1, v0, v1; };  // inclusive tile index range, u0>u1 = empty
+
+__device__ __forceinline__ TileRange chunk_tiles(float4 bb, const ChanParms &cp, int64_t nu, int64_t nv,
+                                                 int ntu, int ntv) {
+    TileRange r{1, 0, 1, 0};
+    if (!(bb.x <= bb.y) || !(bb.z <= bb.w)) return r;
+    float a = bb.x * cp.suh, b = bb.y * cp.suh;
+    float lo_u = fminf(a, b) + (float)(nu / 2), hi_u = fmaxf(a, b) + (float)(nu / 2);
+    a = bb.z * cp.svh;
+    b = bb.w * cp.svh;
+    float lo_v = fminf(a, b) + (float)(nv / 2), hi_v = fmaxf(a, b) + (float)(nv / 2);
+    // nearest cell +- (half support + 2 cells of margin for float rounding)
+    float cl_u = floorf(lo_u + 0.5f) - (SC + 2), ch_u = floorf(hi_u + 0.5f) + (SC + 2);
+    float cl_v = floorf(lo_v + 0.5f) - (SC + 2), ch_v = floorf(hi_v + 0.5f) + (SC + 2);
+    if (!(ch_u >= 0.f) || !(cl_u <= (float)(nu - 1)) || !(ch_v >= 0.f) || !(cl_v <= (float)(nv - 1))) return r;
+    int iu0 = (int)fmaxf(cl_u, 0.f), iu1 = (int)fminf(ch_u, (float)(nu - 1));
+    int iv0 = (int)fmaxf(cl_v, 0.f), iv1 = (int)fminf(ch_v, (float)(nv - 1));
+    r.u0 = iu0 / TU; r.u1 = iu1 / TU; r.v0 = iv0 / TV; r.v1 = iv1 / TV;
+    (void)ntu; (void)ntv;
+    return r;
+}
+
+__global__ void k_count(const float4 *bbox, const ChanParms *chan, int64_t C, int64_t B, int nk,
+                        int64_t nu, int64_t nv, int ntu, int ntv, unsigned *counts) {
+    int64_t ch = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    int64_t n = C * B * nk;
+    if (ch >= n) return;
+    int64_t c = ch / (B * nk);
+    int64_t bk = ch % (B * nk);
+    TileRange r = chunk_tiles(bbox[bk], chan[c], nu, nv, ntu, ntv);
+    unsigned cnt = 0;
+    if (r.u0 <= r.u1 && r.v0 <= r.v1) cnt = (unsigned)((r.u1 - r.u0 + 1) * (r.v1 - r.v0 + 1));
+    counts[ch] = cnt;
+    if (ch == n - 1) counts[n] = 0;  // sentinel: the exclusive scan's last entry is the total
+}
+
+__global__ void k_emit(const float4 *bbox, const ChanParms *chan, int64_t C, int64_t B, int nk, int64_t nu,
+                       int64_t nv, int ntu, int ntv, int continuum, const unsigned long long *offsets,
+                       unsigned long long *keys) {
+    int64_t ch = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    int64_t n = C * B * nk;
+    if (ch >= n) return;
+    int64_t c = ch / (B * nk);
+    int64_t bk = ch % (B * nk);
+    TileRange r = chunk_tiles(bbox[bk], chan[c], nu, nv, ntu, ntv);
+    if (!(r.u0 <= r.u1 && r.v0 <= r.v1)) return;
+    unsigned long long o = offsets[ch];
+    int64_t cimg = continuum ? 0 : c;
+    int64_t NT = (int64_t)ntu * ntv;
+    for (int tu = r.u0; tu <= r.u1; ++tu)
+        for (int tv = r.v0; tv <= r.v1; ++tv) {
+            unsigned long long bin = (unsigned long long)(cimg * NT + (int64_t)tu * ntv + tv);
+            keys[o++] = (bin << 32) | (unsigned long long)ch;
+        }
+}
+
+__global__ void k_bounds(const unsigned long long *keys, int64_t n, int64_t n_bins, int64_t *bin_start) {
+    int64_t bin = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (bin > n_bins) return;
+    unsigned long long target = (unsigned long long)bin << 32;
+    int64_t lo = 0, hi = n;
+    while (lo < hi) {
+        int64_t mid = (lo + hi) >> 1;
+        if (keys[mid] < target) lo = mid + 1; else hi = mid;
+    }
+    bin_start[bin] = lo;
+}
+
+// ---- the tile kernel -------------------------------------------------------
+
+template <int NP, bool CPLX>
+struct Acc;  // per-pol accumulator element
+template <int NP>
+struct Acc<NP, true> { float2 v[NP]; };
+template <int NP>
+struct Acc<NP, false> { float v[NP]; };
+
+__device__ __forceinline__ int mod7(int x) {  // x in [-20, 20] -> [0,7)
+    int r = x % 7;
+    return r < 0 ? r + 7 : r;
+}
+
+__device__ __forceinline__ bool mbar_wait(unsigned addr, unsigned phase) {
+    for (int it = 0; it < (1 << 22); ++it) {
+        unsigned ok;
+        asm volatile(
+            "{\n\t.reg .pred p;\n\t"
+            "mbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\n\t"
+            "selp.u32 %0, 1, 0, p;\n\t}"
+            : "=r"(ok)
+            : "r"(addr), "r"(phase)
+            : "memory");
+        if (ok) return true;
+    }
+    return false;
+}
+
+template <int NP, bool CPLX, bool FFTL>
+__global__ void __launch_bounds__(NW * 32, 2) k_tiles(const TileArgs a) {
+    extern __shared__ __align__(16) unsigned char smem[];
+    // layout: acc tile | table | norm sums | records | misc
+    constexpr int ACC_ELEM = CPLX ? 8 : 4;
+    float *acc_s = reinterpret_cast<float *>(smem);
+    const size_t acc_bytes = (size_t)NP * TU * TV * ACC_ELEM;
+    float *tab = reinterpret_cast<float *>(smem + acc_bytes);
+    float *nsum = tab + ((a.tab_bytes + 3) / 4);
+    const int nsum_len = a.os + 1;
+    unsigned *rec_cuv = reinterpret_cast<unsigned *>(nsum + ((nsum_len + 3) & ~3));
+    int *rec_info = reinterpret_cast<int *>(rec_cuv + NW * NG * ROUND);
+    float4 *rec_wv = reinterpret_cast<float4 *>(rec_info + NW * NG * ROUND);
+    double *sw_part = reinterpret_cast<double *>(rec_wv + NW * NG * ROUND);
+    unsigned long long *mbar = reinterpret_cast<unsigned long long *>(sw_part + NW * 4);
+    int *s_item = reinterpret_cast<int *>(mbar + 1);
+
+    const int tid = threadIdx.x;
+    const int warp = tid >> 5, lane = tid & 31;
+
+    // ---- stage the tap table with a TMA bulk copy -------------------------
+    unsigned mbar_addr = (unsigned)__cvta_generic_to_shared(mbar);
+    if (tid == 0) {
+        asm volatile("mbarrier.init.shared::cta.b64 [%0], 1;" ::"r"(mbar_addr) : "memory");
+        asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
+    }
+    __syncthreads();
+    if (tid == 0) {
+        unsigned dst = (unsigned)__cvta_generic_to_shared(tab);
+        asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;" ::"r"(mbar_addr), "r"(a.tab_bytes)
+                     : "memory");
+        asm volatile(
+            "cp.async.bulk.shared::cluster.global.mbarrier::complete_tx::bytes [%0], [%1], %2, [%3];" ::"r"(dst),
+            "l"(a.tab_g), "r"(a.tab_bytes), "r"(mbar_addr)
+            : "memory");
+    }
+    bool tma_ok = mbar_wait(mbar_addr, 0);
+    if (!tma_ok) {  // bounded wait ran out: load the table with plain loads instead
+        for (int i = tid; i < a.tab_len; i += blockDim.x) tab[i] = a.tab_g[i];
+    }
+    __syncthreads();
+    // norm sums: nsum[o + os/2] = sum_{i=-3..3} tab[|os*i + o|]
+    const int half_os = a.os / 2;
+    for (int i = tid; i < nsum_len; i += blockDim.x) {
+        int o = i - half_os;
+        float s = 0.f;
+        for (int d = -SC; d <= SC; ++d) {
+            int ix = abs(a.os * d + o);
+            s += ix < a.tab_len ? tab[ix] : 0.f;
+        }
+        nsum[i] = s;
+    }
+    // zero the accumulator tile
+    for (int i = tid; i < NP * TU * TV * (CPLX ? 2 : 1); i += blockDim.x) acc_s[i] = 0.f;
+    __syncthreads();
+
+    const int64_t NT = (int64_t)a.ntu * a.ntv;
+    const int64_t n_items = NT * a.n_img;
+    const int cu_c = (int)(a.nu / 2), cv_c = (int)(a.nv / 2);
+    const int g = lane >> 2;          // track processor in the warp
+    const int l4 = lane & 3;          // lane within the processor
+    const int ncol = (l4 < 3) ? 2 : 1;  // column classes l4 and l4+4
+
+    for (;;) {
+        if (tid == 0) *s_item = atomicAdd(a.work_counter, 1);
+        __syncthreads();
+        const int64_t item = *s_item;
+        if (item >= n_items) break;
+        const int64_t tile = item / a.n_img;
+        const int cimg = (int)(item % a.n_img);
+        const int tiu = (int)(tile / a.ntv), tiv = (int)(tile % a.ntv);
+        const int u0 = tiu * TU, v0 = tiv * TV;
+        const int64_t bin = (int64_t)cimg * NT + tile;
+        const int64_t e0 = a.bin_start[bin], e1 = a.bin_start[bin + 1];
+        const int64_t plane = a.nu * a.nv;
+
+        if (e0 < e1) {
+            // ---------------- busy tile ----------------
+            const int64_t n = e1 - e0;
+            const int gi = warp * NG + g;
+            const int64_t rs = e0 + (n * gi) / (NW * NG);
+            const int64_t re = e0 + (n * (gi + 1)) / (NW * NG);
+            int jmax = (int)(re - rs);
+            for (int o = 16; o > 0; o >>= 1) jmax = max(jmax, __shfl_xor_sync(0xffffffffu, jmax, o));
+            // producer ranges for the groups this lane produces for
+            float sw_s[NP], sw_c[NP];
+#pragma unroll
+            for (int p = 0; p < NP; ++p) { sw_s[p] = 0.f; sw_c[p] = 0.f; }
+            // consumer state
+            int prev_cu = -(1 << 28), prev_cv = -(1 << 28);
+            int col[2] = {-(1 << 28), -(1 << 28)};
+            bool colv[2] = {false, false};
+            Acc<NP, CPLX> acc[2][SUP];
+#pragma unroll
+            for (int j = 0; j < 2; ++j)
+#pragma unroll
+                for (int d = 0; d < SUP; ++d)
+#pragma unroll
+                    for (int p = 0; p < NP; ++p) {
+                        if constexpr (CPLX) acc[j][d].v[p] = make_float2(0.f, 0.f);
+                        else acc[j][d].v[p] = 0.f;
+                    }
+
+            auto flush_cell = [&](int j, int d) {
+                int row = prev_cv - SC + d;
+                if (!colv[j] || row < v0 || row >= v0 + TV || row >= a.nv) return;
+                int lu = col[j] - u0, lv = row - v0;
+#pragma unroll
+                for (int p = 0; p < NP; ++p) {
+                    if constexpr (CPLX) {
+                        float2 x = acc[j][d].v[p];
+                        if (x.x != 0.f || x.y != 0.f) {
+                            float *q = acc_s + 2 * (((size_t)p * TU + lu) * TV + lv);
+                            atomicAdd(q, x.x);
+                            atomicAdd(q + 1, x.y);
+                        }
+                    } else {
+                        float x = acc[j][d].v[p];
+                        if (x != 0.f) atomicAdd(acc_s + ((size_t)p * TU + lu) * TV + lv, x);
+                    }
+                }
+            };
+            auto zero_cell = [&](int j, int d) {
+#pragma unroll
+                for (int p = 0; p < NP; ++p) {
+                    if constexpr (CPLX) acc[j][d].v[p] = make_float2(0.f, 0.f);
+                    else acc[j][d].v[p] = 0.f;
+                }
+            };
+
+            unsigned *my_cuv = rec_cuv + warp * NG * ROUND;
+            int *my_info = rec_info + warp * NG * ROUND;
+            float4 *my_wv = rec_wv + warp * NG * ROUND;
+
+            for (int j = 0; j < jmax; ++j) {
+                // decode the chunk of every group for the producer side
+                for (int rnd = 0; rnd < CH / ROUND; ++rnd) {
+                    // ---- producer: 4 records per lane ----
+#pragma unroll
+                    for (int k4 = 0; k4 < 4; ++k4) {
+                        const int r = lane + 32 * k4;
+                        const int gg = r / ROUND, s = r % ROUND;
+                        const int ggi = warp * NG + gg;
+                        const int64_t grs = e0 + (n * ggi) / (NW * NG);
+                        const int64_t gre = e0 + (n * (ggi + 1)) / (NW * NG);
+                        unsigned cuv = 0;
+                        int info = 0;
+                        float4 wv = make_float4(0.f, 0.f, 0.f, 0.f);
+                        if (grs + j < gre) {
+                            const unsigned long long key = a.keys[grs + j];
+                            const int64_t ch = (int64_t)(key & 0xffffffffull);
+                            const int64_t c = ch / (a.B * a.nk);
+                            const int64_t b = (ch / a.nk) % a.B;
+                            const int64_t kk = ch % a.nk;
+                            const int64_t t = kk * CH + rnd * ROUND + s;
+                            if (t < a.T) {
+                                const float4 us = a.uvs[b * a.T + t];
+                                if (!isnan(us.x) && !isnan(us.z)) {
+                                    const ChanParms cp = a.chan[c];
+                                    int cu, ou, cv, ov;
+                                    if (!cell_pair(us.x, us.y, cp.suh, cp.sul, false, cu_c, a.os, cu, ou)) {
+                                        long long i64, o64;
+                                        cell_fp64(a.uvw[(t * a.B + b) * 3 + 0], cp.su, false, cu_c, a.os, i64, o64);
+                                        cu = (int)max(min(i64, (long long)1 << 30), -((long long)1 << 30));
+                                        ou = (int)o64;
+                                    }
+                                    if (!cell_pair(us.z, us.w, cp.svh, cp.svl, false, cv_c, a.os, cv, ov)) {
+                                        long long i64, o64;
+                                        cell_fp64(a.uvw[(t * a.B + b) * 3 + 1], cp.sv, false, cv_c, a.os, i64, o64);
+                                        cv = (int)max(min(i64, (long long)1 << 30), -((long long)1 << 30));
+                                        ov = (int)o64;
+                                    }
+                                    if (cu - SC >= 0 && cu + SC < a.nu && cv - SC >= 0 && cv + SC < a.nv) {
+                                        const int64_t base = ((t * a.B + b) * a.C + c) * a.P + a.p0;
+                                        float w[NP];
+                                        bool pv[NP];
+                                        bool any = false;
+                                        float val[2 * NP];
+#pragma unroll
+                                        for (int p = 0; p < NP; ++p) {
+                                            w[p] = a.weight[base + p];
+                                            if constexpr (CPLX) {
+                                                const float2 vv = a.vis[base + p];
+                                                float xr = vv.x * w[p], xi = vv.y * w[p];
+                                                pv[p] = !isnan(xr) && !isnan(xi) && (xr != 0.f || xi != 0.f);
+                                                val[2 * p] = pv[p] ? xr : 0.f;
+                                                val[2 * p + 1] = pv[p] ? xi : 0.f;
+                                            } else {
+                                                pv[p] = !isnan(w[p]) && w[p] != 0.f;
+                                                val[p] = pv[p] ? w[p] : 0.f;
+                                            }
+                                            any = any || pv[p];
+                                        }
+                                        if (any) {
+                                            if constexpr (CPLX) {
+                                                wv.x = val[0]; wv.y = val[1];
+                                                if (NP > 1) { wv.z = val[2 * (NP - 1)]; wv.w = val[2 * (NP - 1) + 1]; }
+                                            } else {
+                                                wv.x = val[0];
+                                                if (NP > 1) wv.y = val[NP - 1];
+                                            }
+                                            cuv = ((unsigned)cu << 16) | (unsigned)cv;
+                                            info = 1 | ((ou + 1024) << 1) | ((ov + 1024) << 12);
+                                            // sum of weights: home tile only
+                                            if (cu >= u0 && cu < u0 + TU && cv >= v0 && cv < v0 + TV) {
+                                                const float norm = nsum[ou + half_os] * nsum[ov + half_os];
+#pragma unroll
+                                                for (int p = 0; p < NP; ++p) {
+                                                    if (pv[p]) {  // Kahan
+                                                        float y = __fsub_rn(__fmul_rn(w[p], norm), sw_c[p]);
+                                                        float tt = __fadd_rn(sw_s[p], y);
+                                                        sw_c[p] = __fsub_rn(__fsub_rn(tt, sw_s[p]), y);
+                                                        sw_s[p] = tt;
+                                                    }
+                                                }
+                                            }
+                                        }
+                                    }
+                                }
+                            }
+                        }
+                        my_cuv[gg * ROUND + s] = cuv;
+                        my_info[gg * ROUND + s] = info;
+                        my_wv[gg * ROUND + s] = wv;
+                    }
+                    __syncwarp();
+                    // ---- consumer: 16 steps of this processor's chunk ----
+                    for (int s = 0; s < ROUND; ++s) {
+                        const int info = my_info[g * ROUND + s];
+                        if (!(info & 1)) continue;
+                        const unsigned cuv = my_cuv[g * ROUND + s];
+                        const float4 wv = my_wv[g * ROUND + s];
+                        const int cu = (int)(cuv >> 16), cv = (int)(cuv & 0xffffu);
+                        const int ou = ((info >> 1) & 2047) - 1024;
+                        const int ov = ((info >> 12) & 2047) - 1024;
+                        if (cu != prev_cu) {
+#pragma unroll
+                            for (int jj = 0; jj < 2; ++jj) {
+                                if (jj < ncol) {
+                                    const int acls = l4 + 4 * jj;
+                                    const int nc = cu - SC + mod7(acls - (cu - SC));
+                                    if (nc != col[jj]) {
+#pragma unroll
+                                        for (int d = 0; d < SUP; ++d) { flush_cell(jj, d); zero_cell(jj, d); }
+                                        col[jj] = nc;
+                                        colv[jj] = (nc >= u0 && nc < u0 + TU && nc < a.nu);
+                                    }
+                                }
+                            }
+                            prev_cu = cu;
+                        }
+                        if (cv != prev_cv) {
+                            int delta = cv - prev_cv;
+                            if (delta >= SUP || delta <= -SUP) {
+#pragma unroll
+                                for (int jj = 0; jj < 2; ++jj)
+#pragma unroll
+                                    for (int d = 0; d < SUP; ++d) { flush_cell(jj, d); zero_cell(jj, d); }
+                                prev_cv = cv;
+                            } else {
+                                while (delta > 0) {  // window moves to larger v
+#pragma unroll
+                                    for (int jj = 0; jj < 2; ++jj) {
+                                        flush_cell(jj, 0);
+#pragma unroll
+                                        for (int d = 0; d < SUP - 1; ++d) acc[jj][d] = acc[jj][d + 1];
+                                        zero_cell(jj, SUP - 1);
+                                    }
+                                    ++prev_cv;
+                                    --delta;
+                                }
+                                while (delta < 0) {
+#pragma unroll
+                                    for (int jj = 0; jj < 2; ++jj) {
+                                        flush_cell(jj, SUP - 1);
+#pragma unroll
+                                        for (int d = SUP - 1; d > 0; --d) acc[jj][d] = acc[jj][d - 1];
+                                        zero_cell(jj, 0);
+                                    }
+                                    --prev_cv;
+                                    ++delta;
+                                }
+                            }
+                        }
+                        // taps
+                        float tv[SUP];
+#pragma unroll
+                        for (int d = 0; d < SUP; ++d) tv[d] = tab[abs(a.os * (d - SC) + ov)];
+#pragma unroll
+                        for (int jj = 0; jj < 2; ++jj) {
+                            if (jj < ncol) {
+                                const float tu = tab[abs(a.os * (col[jj] - cu) + ou)];
+                                if constexpr (CPLX) {
+                                    const float2 A0 = make_float2(tu * wv.x, tu * wv.y);
+                                    const float2 A1 = make_float2(tu * wv.z, tu * wv.w);
+#pragma unroll
+                                    for (int d = 0; d < SUP; ++d) {
+                                        acc[jj][d].v[0].x = fmaf(A0.x, tv[d], acc[jj][d].v[0].x);
+                                        acc[jj][d].v[0].y = fmaf(A0.y, tv[d], acc[jj][d].v[0].y);
+                                        if (NP > 1) {
+                                            acc[jj][d].v[NP - 1].x = fmaf(A1.x, tv[d], acc[jj][d].v[NP - 1].x);
+                                            acc[jj][d].v[NP - 1].y = fmaf(A1.y, tv[d], acc[jj][d].v[NP - 1].y);
+                                        }
+                                    }
+                                } else {
+                                    const float A0 = tu * wv.x, A1 = tu * wv.y;
+#pragma unroll
+                                    for (int d = 0; d < SUP; ++d) {
+                                        acc[jj][d].v[0] = fmaf(A0, tv[d], acc[jj][d].v[0]);
+                                        if (NP > 1) acc[jj][d].v[NP - 1] = fmaf(A1, tv[d], acc[jj][d].v[NP - 1]);
+                                    }
+                                }
+                            }
+                        }
+                    }
+                    __syncwarp();
+                }
+            }
+            // final flush of the register state
+#pragma unroll
+            for (int jj = 0; jj < 2; ++jj)
+#pragma unroll
+                for (int d = 0; d < SUP; ++d) flush_cell(jj, d);
+            // sum of weights: lane -> warp -> CTA -> global
+#pragma unroll
+            for (int p = 0; p < NP; ++p) {
+                double v = (double)sw_s[p] - (double)sw_c[p];
+                for (int o = 16; o > 0; o >>= 1) v += __shfl_xor_sync(0xffffffffu, v, o);
+                if (lane == 0) sw_part[warp * 4 + p] = v;
+            }
+            __syncthreads();
+            if (tid < NP) {
+                double v = 0.0;
+                for (int w = 0; w < NW; ++w) v += sw_part[w * 4 + tid];
+                if (v != 0.0) atomicAdd(a.sum_weight + (int64_t)cimg * a.P + a.p0 + tid, v);
+            }
+        }
+
+        // ---------------- write the tile (zeros if empty) ----------------
+        const bool busy = e0 < e1;
+        for (int e = tid; e < NP * TU * TV; e += blockDim.x) {
+            const int p = e / (TU * TV);
+            const int r = (e / TV) % TU;
+            const int cl = e % TV;
+            const int u = u0 + r, v = v0 + cl;
+            float2 val = make_float2(0.f, 0.f);
+            if (busy) {
+                if constexpr (CPLX) {
+                    float2 *q = reinterpret_cast<float2 *>(acc_s) + e;
+                    val = *q;
+                    *q = make_float2(0.f, 0.f);
+                } else {
+                    val.x = acc_s[e];
+                    acc_s[e] = 0.f;
+                }
+            }
+            if (u < a.nu && v < a.nv) {
+                int64_t du = u, dv = v;
+                if (FFTL) {  // (x - N/2) mod N for x in [0, N)
+                    du = u < cu_c ? u + (a.nu - cu_c) : u - cu_c;
+                    dv = v < cv_c ? v + (a.nv - cv_c) : v - cv_c;
+                }
+                const int64_t off = ((int64_t)cimg * a.P + a.p0 + p) * plane + du * a.nv + dv;
+                if (CPLX || FFTL) reinterpret_cast<float2 *>(a.grid)[off] = val;
+                else reinterpret_cast<float *>(a.grid)[off] = val.x;
+            }
+        }
+        __syncthreads();
+    }
+}
+
+size_t tile_smem_bytes(int np, bool cplx, int tab_bytes, int os) {
+    size_t acc = (size_t)np * TU * TV * (cplx ? 8 : 4);
+    size_t tab = (size_t)((tab_bytes + 3) / 4) * 4;
+    size_t ns = (size_t)(((os + 1) + 3) & ~3) * 4;
+    size_t rec = (size_t)NW * NG * ROUND * (4 + 4 + 16);
+    size_t misc = NW * 4 * 8 + 8 + 16;
+    return acc + tab + ns + rec + misc;
+}
+
+template <int NP, bool CPLX, bool FFTL>
+int launch_tiles(const TileArgs &ta, cudaStream_t s) {
+    size_t smem = tile_smem_bytes(NP, CPLX, ta.tab_bytes, ta.os);
+    auto kern = k_tiles<NP, CPLX, FFTL>;
+    NGG_CUDA(cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
+    int per_sm = 0;
+    NGG_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, kern, NW * 32, smem));
+    if (per_sm < 1) return fail(NGG_ERR_UNSUPPORTED, "k_tiles does not fit on an SM");
+    int grid = num_sms() * per_sm;
+    kern<<<grid, NW * 32, smem, s>>>(ta);
+    NGG_CHECK_LAUNCH("k_tiles");
+    return NGG_OK;
+}
+
+template <int NP>
+int dispatch_tiles(const TileArgs &ta, bool cplx, bool fftl, cudaStream_t s) {
+    if (cplx) return fftl ? launch_tiles<NP, true, true>(ta, s) : launch_tiles<NP, true, false>(ta, s);
+    return fftl ? launch_tiles<NP, false, true>(ta, s) : launch_tiles<NP, false, false>(ta, s);
+}
+
+__global__ void k_cell_indices(int64_t n_rows, int64_t C, const double *uvw, const double *freq, int64_t nu, int64_t nv,
+                               double dl0, double dl1, int os, int mirror, int32_t *idx, unsigned long long *nfb) {
+    const int64_t id = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (id >= n_rows * C) return;
+    const int64_t r = id / C, c = id % C;
+    double su, sv;
+    uv_scale_dev(freq[c], dl0, dl1, nu, nv, su, sv);
+    const Split a = split_double(su), b = split_double(sv);
+    const double u = uvw[r * 3], v = uvw[r * 3 + 1];
+    const Split x = split_double(u), y = split_double(v);
+    int cu = 0, cv = 0, ou = 0, ov = 0;
+    unsigned long long fb = 0;
+    if (!cell_pair(x.hi, x.lo, a.hi, a.lo, mirror != 0, (int)(nu / 2), os, cu, ou)) {
+        long long i64, o64;
+        cell_fp64(u, su, mirror != 0, (int)(nu / 2), os, i64, o64);
+        cu = (int)max(min(i64, (long long)1 << 30), -((long long)1 << 30));
+        ou = (int)max(min(o64, (long long)1 << 30), -((long long)1 << 30));
+        ++fb;
+    }
+    if (!cell_pair(y.hi, y.lo, b.hi, b.lo, mirror != 0, (int)(nv / 2), os, cv, ov)) {
+        long long i64, o64;
+        cell_fp64(v, sv, mirror != 0, (int)(nv / 2), os, i64, o64);
+        cv = (int)max(min(i64, (long long)1 << 30), -((long long)1 << 30));
+        ov = (int)max(min(o64, (long long)1 << 30), -((long long)1 << 30));
+        ++fb;
+    }
+    idx[id * 4 + 0] = cu;
+    idx[id * 4 + 1] = cv;
+    idx[id * 4 + 2] = ou;
+    idx[id * 4 + 3] = ov;
+    if (fb && nfb) atomicAdd(nfb, fb);
+}
+
+__global__ void k_table(const double *cgk, int n, int npad, float *tab) {
+    int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i < npad) tab[i] = i < n ? (float)cgk[i] : 0.f;
+}
+
+}  // namespace
+
+struct Scratch {
+    std::vector<void *> ptrs;
+    cudaStream_t s;
+    explicit Scratch(cudaStream_t st) : s(st) {}
+    int get(void **p, size_t bytes) {
+        int rc = scratch_alloc(p, bytes, s);
+        if (rc == NGG_OK) ptrs.push_back(*p);
+        return rc;
+    }
+    ~Scratch() {
+        for (void *p : ptrs) scratch_free(p, s);
+    }
+};
+
+}  // namespace ngg
+
+using namespace ngg;
+
+extern "C" int ngg_grid_ps(const NggGridArgs *a, void *stream) {
+    clear_error();
+    if (!a) return fail(NGG_ERR_INVALID, "args is NULL");
+    cudaStream_t s = (cudaStream_t)stream;
+    if (a->mode != NGG_MODE_DATA && a->mode != NGG_MODE_PSF) return fail(NGG_ERR_INVALID, "mode");
+    if (a->chan_mode != NGG_CHAN_CUBE && a->chan_mode != NGG_CHAN_CONTINUUM) return fail(NGG_ERR_INVALID, "chan_mode");
+    if (a->layout != NGG_LAYOUT_NATURAL && a->layout != NGG_LAYOUT_FFT) return fail(NGG_ERR_INVALID, "layout");
+    if (a->support != SUP) return fail(NGG_ERR_UNSUPPORTED, "support must be 7");
+    if (a->oversampling < 1 || a->oversampling > 1000) return fail(NGG_ERR_UNSUPPORTED, "oversampling out of [1,1000]");
+    if (a->n_time < 0 || a->n_baseline < 0 || a->n_chan < 0 || a->n_pol < 1) return fail(NGG_ERR_INVALID, "negative dims");
+    if (a->n_u < 1 || a->n_v < 1 || a->n_u > 65535 || a->n_v > 65535) return fail(NGG_ERR_INVALID, "grid size out of [1,65535]");
+    if (!a->uvw && a->n_time * a->n_baseline > 0) return fail(NGG_ERR_INVALID, "uvw is NULL");
+    if (!a->weight && a->n_time * a->n_baseline * a->n_chan > 0) return fail(NGG_ERR_INVALID, "weight is NULL");
+    if (a->mode == NGG_MODE_DATA && !a->vis && a->n_time * a->n_baseline * a->n_chan > 0)
+        return fail(NGG_ERR_INVALID, "vis is NULL in DATA mode");
+    if (!a->grid || !a->sum_weight || !a->cgk_1D || (!a->freq && a->n_chan > 0)) return fail(NGG_ERR_INVALID, "NULL output/table");
+    const int tab_len = a->oversampling * (a->support / 2 + 1);
+    if (tab_len > MAX_TAB) return fail(NGG_ERR_UNSUPPORTED, "kernel table too long");
+
+    const int64_t T = a->n_time, B = a->n_baseline, C = a->n_chan, P = a->n_pol;
+    const int n_img = a->chan_mode == NGG_CHAN_CONTINUUM ? 1 : (int)C;
+    const bool cplx = a->mode == NGG_MODE_DATA;
+    const bool fftl = a->layout == NGG_LAYOUT_FFT;
+    const size_t elem = (cplx || fftl) ? 8 : 4;
+    const int64_t nu = a->n_u, nv = a->n_v;
+    const int ntu = (int)((nu + TU - 1) / TU), ntv = (int)((nv + TV - 1) / TV);
+    const int nk = (int)((T + CH - 1) / CH);
+
+    if (n_img == 0) return NGG_OK;
+    NGG_CUDA(cudaMemsetAsync(a->sum_weight, 0, sizeof(double) * (size_t)n_img * P, s));
+
+    Scratch sc(s);
+    int rc;
+    const int tab_bytes = ((tab_len * 4 + 15) / 16) * 16;
+    float *tab = nullptr;
+    if ((rc = sc.get((void **)&tab, tab_bytes)) != NGG_OK) return rc;
+    k_table<<<(tab_bytes / 4 + 255) / 256, 256, 0, s>>>(a->cgk_1D, tab_len, tab_bytes / 4, tab);
+    NGG_CHECK_LAUNCH("k_table");
+
+    ChanParms *chan = nullptr;
+    float4 *uvs = nullptr, *bbox = nullptr;
+    if (C > 0 && (rc = sc.get((void **)&chan, sizeof(ChanParms) * C)) != NGG_OK) return rc;
+    const int64_t n_chunks = C * B * nk;
+    int64_t n_keys = 0;
+    unsigned long long *keys_sorted = nullptr;
+    const int64_t n_bins = (int64_t)n_img * ntu * ntv;
+    int64_t *bin_start = nullptr;
+    if ((rc = sc.get((void **)&bin_start, sizeof(int64_t) * (n_bins + 1))) != NGG_OK) return rc;
+
+    if (n_chunks > 0) {
+        if ((rc = sc.get((void **)&uvs, sizeof(float4) * T * B)) != NGG_OK) return rc;
+        if ((rc = sc.get((void **)&bbox, sizeof(float4) * B * nk)) != NGG_OK) return rc;
+        k_chan<<<(int)((C + 127) / 128), 128, 0, s>>>(a->freq, (int)C, a->delta_lm[0], a->delta_lm[1], nu, nv, chan);
+        NGG_CHECK_LAUNCH("k_chan");
+        {
+            int64_t warps = B * nk;
+            k_uvw<<<(unsigned)((warps + 7) / 8), 256, 0, s>>>(a->uvw, T, B, nk, uvs, bbox);
+            NGG_CHECK_LAUNCH("k_uvw");
+        }
+        unsigned *counts = nullptr;
+        unsigned long long *offsets = nullptr;
+        if ((rc = sc.get((void **)&counts, sizeof(unsigned) * (n_chunks + 1))) != NGG_OK) return rc;
+        if ((rc = sc.get((void **)&offsets, sizeof(unsigned long long) * (n_chunks + 1))) != NGG_OK) return rc;
+        const unsigned nb = (unsigned)((n_chunks + 255) / 256);
+        k_count<<<nb, 256, 0, s>>>(bbox, chan, C, B, nk, nu, nv, ntu, ntv, counts);
+        NGG_CHECK_LAUNCH("k_count");
+        size_t tmp_bytes = 0;
+        NGG_CUDA(cub::DeviceScan::ExclusiveSum(nullptr, tmp_bytes, counts, offsets, n_chunks + 1, s));
+        void *tmp = nullptr;
+        if ((rc = sc.get(&tmp, tmp_bytes)) != NGG_OK) return rc;
+        NGG_CUDA(cub::DeviceScan::ExclusiveSum(tmp, tmp_bytes, counts, offsets, n_chunks + 1, s));
+        unsigned long long total = 0;
+        NGG_CUDA(cudaMemcpyAsync(&total, offsets + n_chunks, sizeof(total), cudaMemcpyDeviceToHost, s));
+        NGG_CUDA(cudaStreamSynchronize(s));
+        n_keys = (int64_t)total;
+        if (n_keys > 0) {
+            unsigned long long *keys = nullptr;
+            if ((rc = sc.get((void **)&keys, sizeof(unsigned long long) * n_keys)) != NGG_OK) return rc;
+            if ((rc = sc.get((void **)&keys_sorted, sizeof(unsigned long long) * n_keys)) != NGG_OK) return rc;
+            k_emit<<<nb, 256, 0, s>>>(bbox, chan, C, B, nk, nu, nv, ntu, ntv,
+                                       a->chan_mode == NGG_CHAN_CONTINUUM, offsets, keys);
+            NGG_CHECK_LAUNCH("k_emit");
+            int end_bit = 32;
+            while (end_bit < 64 && ((unsigned long long)n_bins >> (end_bit - 32)) > 0) ++end_bit;
+            size_t sort_bytes = 0;
+            NGG_CUDA(cub::DeviceRadixSort::SortKeys(nullptr, sort_bytes, keys, keys_sorted, n_keys, 0, end_bit, s));
+            void *stmp = nullptr;
+            if ((rc = sc.get(&stmp, sort_bytes)) != NGG_OK) return rc;
+            NGG_CUDA(cub::DeviceRadixSort::SortKeys(stmp, sort_bytes, keys, keys_sorted, n_keys, 0, end_bit, s));
+        }
+    }
+    k_bounds<<<(unsigned)((n_bins + 1 + 255) / 256), 256, 0, s>>>(keys_sorted, n_keys, n_bins, bin_start);
+    NGG_CHECK_LAUNCH("k_bounds");
+
+    int *counter = nullptr;
+    if ((rc = sc.get((void **)&counter, sizeof(int) * 64)) != NGG_OK) return rc;
+
+    TileArgs ta;
+    ta.vis = (const float2 *)a->vis;
+    ta.weight = a->weight;
+    ta.uvw = a->uvw;
+    ta.uvs = uvs;
+    ta.chan = chan;
+    ta.tab_g = tab;
+    ta.keys = keys_sorted;
+    ta.bin_start = bin_start;
+    ta.grid = a->grid;
+    ta.sum_weight = a->sum_weight;
+    ta.T = T; ta.B = B; ta.C = C; ta.P = P;
+    ta.nu = nu; ta.nv = nv;
+    ta.n_img = n_img; ta.ntu = ntu; ta.ntv = ntv; ta.nk = nk;
+    ta.os = a->oversampling;
+    ta.tab_len = tab_len;
+    ta.tab_bytes = tab_bytes;
+    ta.continuum = a->chan_mode == NGG_CHAN_CONTINUUM;
+    (void)elem;
+    for (int64_t p0 = 0, launch = 0; p0 < P; ++launch) {
+        const int np = (P - p0) >= 2 ? 2 : 1;
+        ta.p0 = (int)p0;
+        ta.work_counter = counter + launch;
+        NGG_CUDA(cudaMemsetAsync(ta.work_counter, 0, sizeof(int), s));
+        rc = np == 2 ? dispatch_tiles<2>(ta, cplx, fftl, s) : dispatch_tiles<1>(ta, cplx, fftl, s);
+        if (rc != NGG_OK) return rc;
+        p0 += np;
+        if (launch >= 63) return fail(NGG_ERR_UNSUPPORTED, "too many polarizations");
+    }
+    return NGG_OK;
+}
+
+extern "C" int ngg_cell_indices(int64_t n_rows, int64_t C, const double *uvw, const double *freq, int64_t nu,
+                                int64_t nv, const double delta_lm[2], int os, int mirror, int32_t *idx,
+                                long long *n_fallback, void *stream) {
+    clear_error();
+    cudaStream_t s = (cudaStream_t)stream;
+    if (n_rows < 0 || C < 0 || nu < 1 || nv < 1 || os < 0 || os > 1000 || !delta_lm) return fail(NGG_ERR_INVALID, "dims");
+    if (n_fallback) NGG_CUDA(cudaMemsetAsync(n_fallback, 0, sizeof(long long), s));
+    if (n_rows * C == 0) return NGG_OK;
+    if (!uvw || !freq || !idx) return fail(NGG_ERR_INVALID, "NULL pointer");
+    const int64_t n = n_rows * C;
+    k_cell_indices<<<(unsigned)((n + 255) / 256), 256, 0, s>>>(n_rows, C, uvw, freq, nu, nv, delta_lm[0], delta_lm[1],
+                                                               os, mirror, idx, (unsigned long long *)n_fallback);
+    NGG_CHECK_LAUNCH("k_cell_indices");
+    return NGG_OK;
+}

@@ -1,0 +1,206 @@
+/*
+ * ngg.h -- C ABI of the GB300-native ngcasa imaging hot path (libngg.so).
+ *
+ * Every entry point takes device pointers that the caller owns, a CUDA stream
+ * (cudaStream_t passed as void*, NULL = legacy default stream) and returns an
+ * NGG_* status. Work is enqueued on the stream; results are valid once the
+ * stream has reached that point. Array layouts follow the reference's numpy
+ * arrays (C order): visibilities (time, baseline, chan, pol), uvw
+ * (time, baseline, 3), grids (chan, pol, u, v), images (l, m, chan, pol) --
+ * the same layouts its per-chunk numpy functions take and return.
+ *
+ * Thread safety: calls on different streams may run concurrently; the cuFFT
+ * plan cache is internally locked.
+ */
+#ifndef NGG_H
+#define NGG_H
+
+#include <stddef.h>
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+/* ---- status codes ------------------------------------------------------ */
+#define NGG_OK 0
+#define NGG_ERR_INVALID 1     /* bad argument (shape, null pointer, range)      */
+#define NGG_ERR_NOMEM 2       /* device allocation of scratch failed           */
+#define NGG_ERR_CUDA 3        /* a CUDA runtime / cuFFT call failed            */
+#define NGG_ERR_UNSUPPORTED 4 /* valid request this build does not implement   */
+#define NGG_ERR_TIMEOUT 5     /* a bounded device-side wait ran out            */
+
+/* ---- enumerations ------------------------------------------------------ */
+#define NGG_MODE_DATA 0   /* grid vis*weight into a complex grid               */
+#define NGG_MODE_PSF 1    /* grid weight into a real grid                      */
+
+#define NGG_CHAN_CUBE 0       /* one image channel per visibility channel      */
+#define NGG_CHAN_CONTINUUM 1  /* all channels into image channel 0             */
+
+#define NGG_LAYOUT_NATURAL 0  /* grid[c,p,u,v] as the reference returns it     */
+#define NGG_LAYOUT_FFT 1      /* each plane ifftshift-ed: cell (u,v) stored at
+                                 ((u - Nu/2) mod Nu, (v - Nv/2) mod Nv), the
+                                 input order of an unshifted inverse FFT        */
+
+#define NGG_WEIGHTING_NATURAL 0
+#define NGG_WEIGHTING_UNIFORM 1
+#define NGG_WEIGHTING_BRIGGS 2
+#define NGG_WEIGHTING_BRIGGS_ABS 3
+
+/* Library version, e.g. 100 for 0.1.0. */
+int ngg_version(void);
+/* Message of the last failing call on this host thread ("" when none). */
+const char *ngg_last_error(void);
+
+/* ---- standard (prolate-spheroidal) gridder -------------------------------
+ * Replaces _standard_grid_numpy_wrap / _standard_grid_psf_numpy_wrap and
+ * the loop nest _standard_grid_jit
+ * (ngcasa/imaging/_imaging_utils/_standard_grid.py:123-236, :242-371).
+ *
+ * delta_lm is grid_parms['cell_size'] after _check_grid_parms, i.e. in
+ * radians with delta_lm[0] already negated (_check_imaging_parms.py:38-39).
+ * cgk_1D is the oversampled half-kernel table of length
+ * oversampling*(support/2+1) (_create_prolate_spheroidal_kernel_1D).
+ * weight holds the imaging weights (float32, same shape as vis).
+ * Output grid: complex64 (DATA) or float32 (PSF), shape
+ * (n_chan_img, n_pol, n_u, n_v) where n_chan_img = n_chan (cube) or 1
+ * (continuum); sum_weight float64 (n_chan_img, n_pol). Both are overwritten.
+ * With NGG_LAYOUT_FFT the grid is always complex64 (a PSF grid then has zero
+ * imaginary parts), ready for ngg_fft_correct.
+ * Taps and accumulation are FP32; cell and oversampling indices are the ones
+ * the reference's FP64 arithmetic produces (bit-exact). support must be 7
+ * and oversampling in [1, 1000] in this build.
+ */
+typedef struct NggGridArgs {
+    int mode;          /* NGG_MODE_DATA | NGG_MODE_PSF                         */
+    int chan_mode;     /* NGG_CHAN_CUBE | NGG_CHAN_CONTINUUM                   */
+    int layout;        /* NGG_LAYOUT_NATURAL | NGG_LAYOUT_FFT                  */
+    int support;
+    int oversampling;
+    int reserved0;
+    int64_t n_time, n_baseline, n_chan, n_pol;
+    int64_t n_u, n_v;  /* padded grid size (image_size_padded)                */
+    double delta_lm[2];
+    const void *vis;      /* complex64 (T,B,C,P); NULL for PSF                 */
+    const double *uvw;    /* float64 (T,B,3) metres                            */
+    const float *weight;  /* float32 (T,B,C,P)                                 */
+    const double *freq;   /* float64 (C) Hz                                    */
+    const double *cgk_1D; /* float64 (oversampling*(support/2+1))              */
+    void *grid;           /* complex64 / float32 (Cimg,P,Nu,Nv)                */
+    double *sum_weight;   /* float64 (Cimg,P)                                  */
+} NggGridArgs;
+
+int ngg_grid_ps(const NggGridArgs *args, void *stream);
+
+/* Cell and oversampling-offset indices as every kernel above computes them
+ * (the FP32-pair evaluation with FP64 fallback): for each uvw row r and
+ * channel c, idx[(r*n_chan + c)*4 + {0,1,2,3}] = (cu, cv, ou, ov), with
+ * cu = int(u_pos + 0.5), ou = floor((cu - u_pos)*oversampling + 0.5) and
+ * likewise for v (_standard_grid.py:299-324), mirrored (-u, -v) when
+ * mirror != 0. n_fallback (device int64, may be NULL) receives the number of
+ * coordinates that needed the FP64 path. For verification and tooling. */
+int ngg_cell_indices(int64_t n_rows, int64_t n_chan, const double *uvw, const double *freq,
+                     int64_t n_u, int64_t n_v, const double delta_lm[2], int oversampling,
+                     int mirror, int32_t *idx, long long *n_fallback, void *stream);
+
+/* ---- imaging weights ------------------------------------------------------
+ * Weight-density grid: replaces the do_imaging_weight branch of
+ * _standard_grid_jit as called by calc_briggs_weights
+ * (make_imaging_weight.py:153-161; _standard_grid.py:327-333, 349-369):
+ * unpadded n_u x n_v grid, nearest cell, the mirrored cell (-u,-v) also
+ * incremented, weights of two or more pols averaged over pols 0 and 1.
+ * Because every pol then receives the same value, the reference's
+ * (chan, pol, u, v) density grid has identical planes for all pols; this call
+ * writes that plane once: density float32 (n_chan_img, n_u, n_v) and
+ * density_sum_weight float64 (n_chan_img) (which the reference also stores
+ * per pol, identically). Mirrored cells that fall off the grid (only
+ * possible for centre cells 0 or 1 at the edge) are dropped.
+ */
+int ngg_grid_density(int chan_mode, int64_t n_time, int64_t n_baseline, int64_t n_chan,
+                     int64_t n_pol, int64_t n_u, int64_t n_v, const double delta_lm[2],
+                     const double *uvw, const float *weight, const double *freq,
+                     float *density, double *density_sum_weight, void *stream);
+
+/* Briggs / uniform factors: replaces calculate_briggs_parms
+ * (make_imaging_weight.py:198-213). factors float64 (2, n_chan_img):
+ * briggs: f0 = (5*10^-robust)^2 / (sum(W^2)/sum_weight), f1 = 1;
+ * uniform: f0 = 1, f1 = 0; briggs_abs: f0 = robust^2, f1 = 2*noise^2 (the
+ * documented intent; the reference's branch raises NameError). */
+int ngg_briggs_factors(int weighting, double robust, double briggs_abs_noise,
+                       int64_t n_chan_img, int64_t n_u, int64_t n_v, const float *density,
+                       const double *density_sum_weight, double *factors, void *stream);
+
+/* Imaging-weight lookup: replaces _standard_imaging_weight_degrid_numpy_wrap
+ * and _standard_imaging_weight_degrid_jit (_standard_grid.py:443-518).
+ * imaging_weight float32 (T,B,C,P): two-pol average of weight divided by
+ * f0*W[cell]+f1 where the pol's own weight and W are finite and non-zero;
+ * 0 where the nearest cell is off the grid or uvw is NaN. */
+int ngg_weight_lookup(int chan_mode, int64_t n_time, int64_t n_baseline, int64_t n_chan,
+                      int64_t n_pol, int64_t n_u, int64_t n_v, const double delta_lm[2],
+                      const double *uvw, const float *weight, const double *freq,
+                      const float *density, const double *factors, float *imaging_weight,
+                      void *stream);
+
+/* ---- FFT, crop and gridding correction ------------------------------------
+ * Replaces the tail of make_image / make_psf (make_image.py:116-130,
+ * make_psf.py:117-131): image = Re(fftshift(ifft2(ifftshift(grid))))*Nu*Nv
+ * cropped to the centre (n_l, n_m) window (_remove_padding.py:20-31),
+ * divided by sum_weight (0 -> 1) and by correction[l,m] (the cropped
+ * grid-correction image). grid is a stack of n_chan_img*n_pol complex64
+ * planes in NGG_LAYOUT_FFT order; it is transformed IN PLACE (destroyed).
+ * image float64 (n_l, n_m, n_chan_img, n_pol).
+ * correction float64 (n_l, n_m); sum_weight float64 (n_chan_img, n_pol). */
+int ngg_fft_correct(void *grid, int64_t n_chan_img, int64_t n_pol,
+                    int64_t n_u, int64_t n_v, int64_t n_l, int64_t n_m,
+                    const double *sum_weight, const double *correction, double *image,
+                    void *stream);
+
+/* ---- degridding: the exact adjoint of the imaging operator ---------------
+ * The reference has no visibility degridder (_graph_standard_degrid prints
+ * "Degridding of visibilities and psf still needs to be implemented",
+ * _standard_grid.py:429-430); these two calls are the adjoints of
+ * ngg_fft_correct and of ngg_grid_ps (DATA mode) so that
+ * make_image = fft_correct . grid_ps has the transpose
+ * degrid_ps . fft_correct_adjoint (real inner product on images, complex on
+ * visibilities).
+ *
+ * ngg_fft_correct_adjoint: image (n_l, n_m, n_chan_img, n_pol), float32 or
+ * float64 (image_is_f64), is divided by sum_weight (0 -> 1) and correction,
+ * placed at the cropped window of zeroed padded planes in NGG_LAYOUT_FFT
+ * order, and forward-transformed (unnormalised, e^{-i}) in place: grid
+ * complex64 (n_chan_img, n_pol, n_u, n_v) in NGG_LAYOUT_FFT order.
+ *
+ * ngg_degrid_ps: vis[t,b,c,p] = weight[t,b,c,p] * sum_taps conv * grid[cell]
+ * over the same 7x7 footprint, cells and oversampling offsets as
+ * ngg_grid_ps; 0 where the footprint leaves the grid or uvw is NaN. weight
+ * may be NULL (all ones). grid layout given by `layout`. */
+typedef struct NggDegridArgs {
+    int chan_mode;
+    int layout;
+    int support;
+    int oversampling;
+    int64_t n_time, n_baseline, n_chan, n_pol;
+    int64_t n_u, n_v;
+    double delta_lm[2];
+    const void *grid;     /* complex64 (Cimg,P,Nu,Nv)                           */
+    const double *uvw;    /* float64 (T,B,3)                                    */
+    const float *weight;  /* float32 (T,B,C,P) or NULL                          */
+    const double *freq;   /* float64 (C)                                        */
+    const double *cgk_1D; /* float64 (oversampling*(support/2+1))               */
+    void *vis;            /* complex64 (T,B,C,P) output                         */
+} NggDegridArgs;
+
+int ngg_degrid_ps(const NggDegridArgs *args, void *stream);
+
+int ngg_fft_correct_adjoint(const void *image, int image_is_f64, int64_t n_chan_img, int64_t n_pol,
+                            int64_t n_u, int64_t n_v, int64_t n_l, int64_t n_m,
+                            const double *sum_weight, const double *correction, void *grid,
+                            void *stream);
+
+/* Release cached cuFFT plans and scratch held by the library. */
+void ngg_release_cache(void);
+
+#ifdef __cplusplus
+}
+#endif
+#endif /* NGG_H */

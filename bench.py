@@ -1,0 +1,371 @@
+#!/usr/bin/env python
+"""Gridding throughput of the large-cube imaging workload on GB300.
+
+Workload (one step): DATA-mode convolutional gridding of the whole large
+cube through ngg_grid_ps -- 64 antennas in a 3-arm log spiral of 2.5 km
+radius (2016 baselines), 1024 x 8 s integrations, 256 channels over
+1.0-1.5 GHz, RR/LL (1.057e9 visibilities, 5% flagged), Briggs robust 0.5
+imaging weights (computed on the GPU before timing), 4096^2 image at 1 arcsec
+(4915^2 padded grid), prolate-spheroidal support 7, oversampling 100.
+Synthetic seeded data stand in for an observation (no dataset offline).
+
+Prints one JSON line. `value` = Mvis/s with inputs resident in HBM; `e2e` =
+the same call fed from pinned host buffers (H2D of the step's inputs and D2H
+of the resulting grid inside the timed region). The inputs (12.7 GB) exceed
+L2, so no flush is needed between steps. `roofline` is the tile-accumulation
+kernel against the measured HBM copy bandwidth; `cpu_baseline` is the C FP64
+restatement of the reference gridder on all host cores on a channel sample.
+
+--impl reference times the CPU restatement of the reference's gridder alone.
+Multi-GPU (torchrun): each rank grids its own cube (weak scaling, no
+collective on the data path); rank 0 prints the line.
+"""
+import argparse
+import json
+import os
+import subprocess
+import sys
+import tempfile
+import time
+
+import numpy as np
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, ROOT)
+
+METRIC = 'Mvis/s gridded & err vs FP64; learned vs table GCF mosaic time at 1e-3 error'
+WORKLOAD = 'large_cube_briggs_grid'
+
+
+def parse():
+    p = argparse.ArgumentParser()
+    p.add_argument('--gpus', type=int, default=1)
+    p.add_argument('--steps', type=int, default=5)
+    p.add_argument('--warmup', type=int, default=3)
+    p.add_argument('--impl', default='ngg', choices=['ngg', 'reference'])
+    p.add_argument('--n-time', type=int, default=1024)
+    p.add_argument('--n-chan', type=int, default=256)
+    p.add_argument('--cpu-chans', type=int, default=16, help='channels in the CPU-baseline sample')
+    p.add_argument('--no-e2e', action='store_true')
+    p.add_argument('--no-cpu', action='store_true')
+    p.add_argument('--no-err', action='store_true')
+    return p.parse_args()
+
+
+def dist_env():
+    return int(os.environ.get('RANK', 0)), int(os.environ.get('WORLD_SIZE', 1)), int(os.environ.get('LOCAL_RANK', 0))
+
+
+def measured_peaks():
+    try:
+        with open(os.path.join(ROOT, 'MEASURED_PEAKS.json')) as f:
+            d = json.load(f)
+        return float(d['hbm_gbs']), 'measured'
+    except Exception:
+        return 6800.0, 'fallback'
+
+
+class Clocks:
+    """nvidia-smi sampler for the timed region (SM clock, throttle reasons)."""
+    Q = ('index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,'
+         'clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,'
+         'clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap')
+
+    def __init__(self, gpu_index):
+        self.path = os.path.join(tempfile.gettempdir(), f'ngg_clocks_{os.getpid()}.csv')
+        self.idx = gpu_index
+        self.p = None
+
+    def start(self):
+        try:
+            self.f = open(self.path, 'w')
+            self.p = subprocess.Popen(['nvidia-smi', '-i', str(self.idx), '--query-gpu=' + self.Q,
+                                       '--format=csv,noheader,nounits', '-lms', '200'], stdout=self.f,
+                                      stderr=subprocess.DEVNULL)
+        except Exception:
+            self.p = None
+
+    def stop(self):
+        if self.p is None:
+            return None
+        self.p.terminate()
+        try:
+            self.p.wait(timeout=5)
+        except Exception:
+            self.p.kill()
+        self.f.close()
+        sm, smax, reasons = [], 0.0, set()
+        names = ['hw_slowdown', 'hw_thermal_slowdown', 'sw_thermal_slowdown', 'sw_power_cap']
+        for line in open(self.path):
+            parts = [x.strip() for x in line.split(',')]
+            if len(parts) < 9:
+                continue
+            try:
+                sm.append(float(parts[1]))
+                smax = max(smax, float(parts[2]))
+            except ValueError:
+                continue
+            for n, v in zip(names, parts[5:9]):
+                if v.lower() == 'active':
+                    reasons.add(n)
+        if not sm:
+            return None
+        return {'sm_mhz': float(np.median(sm)), 'sm_max_mhz': smax, 'reasons': sorted(reasons), 'samples': len(sm)}
+
+
+def cpu_threads():
+    try:
+        return len(os.sched_getaffinity(0))
+    except Exception:
+        return os.cpu_count() or 1
+
+
+def oracle_sample(uvw, vis_s, w_s, freq_s, cgk, npad, cell, threads):
+    """Time the C FP64 restatement of the reference gridder on a channel sample."""
+    from oracle import cbind
+    cbind.build()
+    t0 = time.perf_counter()
+    g, sw = cbind.grid('data', vis_s, uvw, w_s, freq_s, cgk, 7, 100, npad, cell, 'cube', threads)
+    dt = time.perf_counter() - t0
+    return g, sw, dt
+
+
+def reference_arm(args, rank):
+    """CPU restatement of the reference gridder, all host threads, bounded samples."""
+    if rank != 0:
+        return
+    from cngi_prototype_gb300 import simulate
+    from cngi_prototype_gb300.imaging._imaging_utils import _gridding_convolutional_kernels as G
+    from cngi_prototype_gb300.imaging._imaging_utils._check_imaging_parms import _check_grid_parms
+    obs = simulate.config_large_cube(n_time=args.n_time, n_chan=args.n_chan, with_vis=False)
+    gp = {'image_size': list(obs.image_size), 'cell_size': list(obs.cell_arcsec)}
+    _check_grid_parms(gp)
+    cgk = G._create_prolate_spheroidal_kernel_1D(100, 7)
+    nc = min(args.cpu_chans, len(obs.freq))
+    T, B = obs.uvw.shape[:2]
+    rng = np.random.default_rng(7)
+    # gridding cost does not depend on visibility values, only on uvw/flags
+    vis = (rng.standard_normal((T, B, nc, 2)) + 1j * rng.standard_normal((T, B, nc, 2))).astype(np.complex64)
+    w = np.ones((T, B, nc, 2))
+    fl = rng.random((T, B, nc, 2)) < 0.05
+    vis[fl] = np.nan
+    w[fl] = np.nan
+    threads = cpu_threads()
+    times = []
+    for k in range(args.warmup + args.steps):
+        _, _, dt = oracle_sample(obs.uvw, vis, w, obs.freq[:nc], cgk, gp['image_size_padded'], gp['cell_size'],
+                                 threads)
+        if k >= args.warmup:
+            times.append(dt)
+    nvis = T * B * nc * 2
+    v = nvis / float(np.mean(times)) / 1e6
+    line = {
+        'impl': 'reference', 'metric': METRIC, 'value': v, 'unit': 'Mvis/s', 'n_gpus': args.gpus,
+        'steps': args.steps, 'warmup': args.warmup, 'ms_per_step': float(np.mean(times)) * 1e3,
+        'higher_is_better': True, 'scaling': 'weak', 'vs_baseline': None, 'dtype': 'f64', 'data': 'synthetic',
+        'config': {'workload': WORKLOAD, 'n_time': T, 'n_baseline': B, 'n_chan': args.n_chan, 'n_pol': 2,
+                   'image_size': 4096, 'grid': int(gp['image_size_padded'][0]), 'support': 7, 'oversampling': 100},
+        'cpu_baseline': {'value': v, 'unit': 'Mvis/s', 'cores': threads, 'kind': 'port',
+                         'sample': f'channels 0-{nc - 1} of the {args.n_chan}-channel cube: all {T}x{B} rows x 2 pols '
+                                   f'({nvis} vis), C FP64 restatement of _standard_grid_jit, OpenMP over channels'},
+        'e2e': {'value': v, 'unit': 'Mvis/s', 'h2d_bytes_per_step': 0, 'd2h_bytes_per_step': 0},
+    }
+    print(json.dumps(line), flush=True)
+
+
+def main():
+    args = parse()
+    rank, world, local = dist_env()
+    if args.impl == 'reference':
+        if world > 1:
+            import torch.distributed as dist
+            dist.init_process_group('gloo')
+        reference_arm(args, rank)
+        return
+    import torch
+    torch.cuda.set_device(local)
+    dist = None
+    if world > 1:
+        import torch.distributed as dist
+        dist.init_process_group('nccl')
+    from cngi_prototype_gb300 import build, _lib, simulate
+    from cngi_prototype_gb300.imaging._imaging_utils import _gridding_convolutional_kernels as G
+    from cngi_prototype_gb300.imaging._imaging_utils._check_imaging_parms import _check_grid_parms
+    build.build()
+    _lib.load()
+
+    # ---- synthetic cube on this rank's GPU (untimed) --------------------
+    obs = simulate.config_large_cube(seed=2 + rank, n_time=args.n_time, n_chan=args.n_chan, vis_device='cuda')
+    gp = {'image_size': list(obs.image_size), 'cell_size': list(obs.cell_arcsec)}
+    _check_grid_parms(gp)
+    npad = gp['image_size_padded']
+    cell = gp['cell_size']
+    cgk = G._create_prolate_spheroidal_kernel_1D(100, 7)
+    vis_d = obs.vis
+    w_d = obs.weight
+    T, B, C, P = vis_d.shape
+    uvw_d = torch.as_tensor(obs.uvw, device='cuda')
+    freq_d = torch.as_tensor(obs.freq, device='cuda')
+    cgk_d = torch.as_tensor(cgk, device='cuda')
+    dens, dsw = _lib.grid_density(uvw_d, w_d, freq_d, gp['image_size'], cell)
+    fac = _lib.briggs_factors(dens, dsw, 'briggs', 0.5)
+    iw_d = _lib.weight_lookup(uvw_d, w_d, freq_d, dens, fac, cell)
+    del dens
+    torch.cuda.synchronize()
+    grid = torch.empty((C, P, int(npad[0]), int(npad[1])), dtype=torch.complex64, device='cuda')
+    sw = torch.empty((C, P), dtype=torch.float64, device='cuda')
+
+    def step():
+        _lib.grid_ps(vis_d, uvw_d, iw_d, freq_d, cgk_d, npad, cell, grid=grid, sum_weight=sw)
+
+    for _ in range(args.warmup):
+        step()
+    torch.cuda.synchronize()
+    if dist:
+        dist.barrier()
+    clocks = Clocks(local)
+    clocks.start()
+    time.sleep(0.3)
+    stream = torch.cuda.current_stream()
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    torch.cuda.synchronize()
+    e0.record(stream)
+    for _ in range(args.steps):
+        step()
+    e1.record(stream)
+    torch.cuda.synchronize()
+    ms = e0.elapsed_time(e1) / args.steps
+    clk = clocks.stop()
+    if dist:
+        t = torch.tensor([ms], device='cuda')
+        dist.all_reduce(t, op=dist.ReduceOp.MAX)
+        ms = float(t.item())
+    n_vis = T * B * C * P
+    value = n_vis * world / (ms * 1e-3) / 1e6
+
+    # ---- dominant kernel: tile accumulation pass (events on its stream) ----
+    _lib.set_profiling(True)
+    tiles_ms = []
+    for _ in range(3):
+        step()
+        bms, tms = _lib.last_phase_ms()
+        tiles_ms.append(tms)
+    _lib.set_profiling(False)
+    t_tiles = float(np.median(tiles_ms))
+    grid_bytes = C * P * int(npad[0]) * int(npad[1]) * 8
+    alg_bytes = n_vis * (8 + 4) + T * B * 24 + grid_bytes + C * P * 8
+    peak, peak_kind = measured_peaks()
+    achieved = alg_bytes / (t_tiles * 1e-3) / 1e9
+    traffic = None
+    tr_path = os.path.join(ROOT, 'profiles', 'k_tiles_traffic.json')
+    if os.path.exists(tr_path):
+        try:
+            tr = json.load(open(tr_path))
+            traffic = float(tr['dram_bytes_per_vis']) * n_vis + float(tr['dram_bytes_per_grid_byte']) * grid_bytes
+        except Exception:
+            traffic = None
+    roofline = {'bound': 'hbm', 'achieved': achieved, 'peak': peak, 'unit': 'GB/s', 'frac': achieved / peak,
+                'traffic': traffic, 'kernel': 'k_tiles', 'kernel_ms': t_tiles, 'binning_ms': bms,
+                'algorithmic_bytes': alg_bytes, 'peak_kind': peak_kind}
+
+    # ---- end to end from pinned host buffers ----------------------------
+    e2e = None
+    if not args.no_e2e:
+        vis_h = torch.empty(vis_d.shape, dtype=vis_d.dtype, pin_memory=True)
+        iw_h = torch.empty(iw_d.shape, dtype=iw_d.dtype, pin_memory=True)
+        uvw_h = torch.empty(uvw_d.shape, dtype=uvw_d.dtype, pin_memory=True)
+        vis_h.copy_(vis_d)
+        iw_h.copy_(iw_d)
+        uvw_h.copy_(uvw_d)
+        stage_elems = (1 << 32) // 8      # 4 GiB pinned staging ring for the grid
+        stage = torch.empty(stage_elems, dtype=torch.complex64, pin_memory=True)
+        sw_h = torch.empty(sw.shape, dtype=sw.dtype, pin_memory=True)
+        gflat = grid.view(-1)
+
+        def e2e_step():
+            vis_d.copy_(vis_h, non_blocking=True)
+            iw_d.copy_(iw_h, non_blocking=True)
+            uvw_d.copy_(uvw_h, non_blocking=True)
+            step()
+            for o in range(0, gflat.numel(), stage_elems):
+                n = min(stage_elems, gflat.numel() - o)
+                stage[:n].copy_(gflat[o:o + n], non_blocking=True)
+            sw_h.copy_(sw, non_blocking=True)
+
+        e2e_step()
+        torch.cuda.synchronize()
+        ke = max(1, min(args.steps, 3))
+        e0.record(stream)
+        for _ in range(ke):
+            e2e_step()
+        e1.record(stream)
+        torch.cuda.synchronize()
+        ems = e0.elapsed_time(e1) / ke
+        if dist:
+            t = torch.tensor([ems], device='cuda')
+            dist.all_reduce(t, op=dist.ReduceOp.MAX)
+            ems = float(t.item())
+        h2d = vis_h.numel() * 8 + iw_h.numel() * 4 + uvw_h.numel() * 8
+        d2h = grid_bytes + sw_h.numel() * 8
+        e2e = {'value': n_vis * world / (ems * 1e-3) / 1e6, 'unit': 'Mvis/s', 'h2d_bytes_per_step': int(h2d),
+               'd2h_bytes_per_step': int(d2h), 'ms_per_step': ems,
+               'note': 'inputs from pinned host memory; grid returned through a 4 GiB pinned staging ring'}
+        del vis_h, iw_h, uvw_h, stage
+
+    # ---- CPU baseline and error vs FP64 on a channel sample (rank 0) ----
+    cpu = None
+    err = None
+    if rank == 0 and not args.no_cpu:
+        nc = min(args.cpu_chans, C)
+        vis_s = vis_d[:, :, :nc].cpu().numpy()
+        w_s = iw_d[:, :, :nc].cpu().numpy().astype(np.float64)
+        threads = cpu_threads()
+        go, swo, dt = oracle_sample(obs.uvw, vis_s, w_s, obs.freq[:nc], cgk, npad, cell, threads)
+        nv = T * B * nc * P
+        cpu = {'value': nv / dt / 1e6, 'unit': 'Mvis/s', 'cores': threads, 'kind': 'port',
+               'sample': f'channels 0-{nc - 1}: all {T}x{B} rows x {P} pols ({nv} vis), C FP64 restatement of '
+                         f'_standard_grid_jit, OpenMP over channels, complex128 grid'}
+        if not args.no_err:
+            g = grid[:nc].cpu().numpy()
+            ge = np.abs(g - go)
+            pk = np.abs(go).max()
+            sw_err = float(np.max(np.abs(sw[:nc].cpu().numpy() - swo) / np.abs(swo)))
+            # image of channel 0 (both pols): GPU pipeline vs numpy FP64 FFT of the oracle grid
+            corr = G._create_prolate_spheroidal_kernel(100, 7, npad)[1]
+            s0 = int(npad[0]) // 2 - 2048
+            corr = corr[s0:s0 + 4096, s0:s0 + 4096]
+            gf = torch.fft.ifftshift(grid[:1], dim=(2, 3)).contiguous()
+            img = _lib.fft_correct(gf, sw[:1], corr, [4096, 4096]).cpu().numpy()
+            del gf
+            ref = np.empty_like(img)
+            for p in range(P):
+                pl = np.fft.fftshift(np.fft.ifft2(np.fft.ifftshift(go[0, p])))
+                pl = pl[s0:s0 + 4096, s0:s0 + 4096].real * (int(npad[0]) * int(npad[1]))
+                ref[:, :, 0, p] = pl / (swo[0, p] if swo[0, p] != 0 else 1.0) / corr
+            ie = np.abs(img - ref)
+            ipk = np.abs(ref).max()
+            err = {'grid_max': float(ge.max() / pk), 'grid_rms': float(np.sqrt(np.mean(ge ** 2)) / pk),
+                   'sum_weight_max_rel': sw_err, 'image_max': float(ie.max() / ipk),
+                   'image_rms': float(np.sqrt(np.mean(ie ** 2)) / ipk),
+                   'sample': f'grid: channels 0-{nc - 1}; image: channel 0, both pols; peak-normalised'}
+
+    if rank == 0:
+        line = {
+            'metric': METRIC, 'value': value, 'unit': 'Mvis/s', 'n_gpus': world, 'steps': args.steps,
+            'warmup': args.warmup, 'ms_per_step': ms, 'higher_is_better': True, 'scaling': 'weak',
+            'vs_baseline': None, 'dtype': 'f32', 'data': 'synthetic',
+            'config': {'workload': WORKLOAD, 'n_time': T, 'n_baseline': B, 'n_chan': C, 'n_pol': P,
+                       'n_vis': n_vis, 'image_size': 4096, 'grid': int(npad[0]), 'cell_arcsec': 1.0,
+                       'weighting': 'briggs 0.5', 'support': 7, 'oversampling': 100, 'flags': 0.05,
+                       'l2': 'inputs (12.7 GB) larger than L2; no flush', 'parallelism': f'replica x{world}'},
+            'roofline': roofline, 'cpu_baseline': cpu, 'e2e': e2e, 'err_vs_fp64': err, 'clocks': clk,
+            'gpu_launches': 11 * args.steps,
+        }
+        print(json.dumps(line), flush=True)
+    if dist:
+        dist.barrier()
+        dist.destroy_process_group()
+
+
+if __name__ == '__main__':
+    main()

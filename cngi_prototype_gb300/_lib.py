@@ -58,6 +58,8 @@ SIGNATURES = {
     'ngg_degrid_ps': (ctypes.c_int, [ctypes.POINTER(NggDegridArgs), _vp]),
     'ngg_cell_indices': (ctypes.c_int, [_i64, _i64, _vp, _vp, _i64, _i64, ctypes.POINTER(ctypes.c_double),
                                         ctypes.c_int, ctypes.c_int, _vp, _vp, _vp]),
+    'ngg_set_profiling': (None, [ctypes.c_int]),
+    'ngg_last_phase_ms': (ctypes.c_int, [ctypes.POINTER(ctypes.c_double), ctypes.POINTER(ctypes.c_double)]),
     'ngg_release_cache': (None, []),
 }
 
@@ -280,3 +282,14 @@ def cell_indices(uvw_rows, freq, n_uv, delta_lm, oversampling, mirror=False):
                                    int(oversampling), 1 if mirror else 0, _ptr(idx), _ptr(nfb), _stream()),
            'ngg_cell_indices')
     return idx, int(nfb.item())
+
+
+def set_profiling(enable=True):
+    load().ngg_set_profiling(1 if enable else 0)
+
+
+def last_phase_ms():
+    """(binning_ms, tiles_ms) of the last profiled ngg_grid_ps call on this thread."""
+    a, b = ctypes.c_double(), ctypes.c_double()
+    _check(load().ngg_last_phase_ms(ctypes.byref(a), ctypes.byref(b)), 'ngg_last_phase_ms')
+    return a.value, b.value

@@ -669,9 +669,40 @@ struct Scratch {
     }
 };
 
+struct Prof {
+    bool on = false;
+    bool valid = false;
+    cudaEvent_t ev[3] = {nullptr, nullptr, nullptr};
+};
+static thread_local Prof g_prof;
+
+static void prof_record(int i, cudaStream_t s) {
+    if (!g_prof.on) return;
+    if (!g_prof.ev[i]) cudaEventCreate(&g_prof.ev[i]);
+    cudaEventRecord(g_prof.ev[i], s);
+    if (i == 2) g_prof.valid = true;
+}
+
 }  // namespace ngg
 
 using namespace ngg;
+
+extern "C" void ngg_set_profiling(int enable) {
+    g_prof.on = enable != 0;
+    g_prof.valid = false;
+}
+
+extern "C" int ngg_last_phase_ms(double *binning_ms, double *tiles_ms) {
+    clear_error();
+    if (!g_prof.valid) return fail(NGG_ERR_INVALID, "no profiled ngg_grid_ps call on this thread");
+    NGG_CUDA(cudaEventSynchronize(g_prof.ev[2]));
+    float a = 0.f, b = 0.f;
+    NGG_CUDA(cudaEventElapsedTime(&a, g_prof.ev[0], g_prof.ev[1]));
+    NGG_CUDA(cudaEventElapsedTime(&b, g_prof.ev[1], g_prof.ev[2]));
+    if (binning_ms) *binning_ms = a;
+    if (tiles_ms) *tiles_ms = b;
+    return NGG_OK;
+}
 
 extern "C" int ngg_grid_ps(const NggGridArgs *a, void *stream) {
     clear_error();
@@ -702,6 +733,8 @@ extern "C" int ngg_grid_ps(const NggGridArgs *a, void *stream) {
     const int nk = (int)((T + CH - 1) / CH);
 
     if (n_img == 0) return NGG_OK;
+    g_prof.valid = false;
+    prof_record(0, s);
     NGG_CUDA(cudaMemsetAsync(a->sum_weight, 0, sizeof(double) * (size_t)n_img * P, s));
 
     Scratch sc(s);
@@ -769,6 +802,8 @@ extern "C" int ngg_grid_ps(const NggGridArgs *a, void *stream) {
 
     int *counter = nullptr;
     if ((rc = sc.get((void **)&counter, sizeof(int) * 64)) != NGG_OK) return rc;
+    NGG_CUDA(cudaMemsetAsync(counter, 0, sizeof(int) * 64, s));
+    prof_record(1, s);
 
     TileArgs ta;
     ta.vis = (const float2 *)a->vis;
@@ -793,12 +828,12 @@ extern "C" int ngg_grid_ps(const NggGridArgs *a, void *stream) {
         const int np = (P - p0) >= 2 ? 2 : 1;
         ta.p0 = (int)p0;
         ta.work_counter = counter + launch;
-        NGG_CUDA(cudaMemsetAsync(ta.work_counter, 0, sizeof(int), s));
         rc = np == 2 ? dispatch_tiles<2>(ta, cplx, fftl, s) : dispatch_tiles<1>(ta, cplx, fftl, s);
         if (rc != NGG_OK) return rc;
         p0 += np;
         if (launch >= 63) return fail(NGG_ERR_UNSUPPORTED, "too many polarizations");
     }
+    prof_record(2, s);
     return NGG_OK;
 }
 

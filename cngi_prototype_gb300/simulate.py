@@ -129,6 +129,47 @@ def point_source_vis(uvw, freq, l, m, flux, n_pol=2, noise_sigma=0.0, rng=None,
     return vis
 
 
+def point_source_vis_torch(uvw, freq, l, m, flux, n_pol, noise_sigma, seed, device='cuda'):
+    """Large-cube generator on the GPU: (T,B,C,P) complex64 torch tensor.
+
+    The phase 2 pi f (u l + v m)/c is formed and range-reduced in FP64 per
+    (row, source, channel) and evaluated with FP32 sin/cos; noise is drawn
+    per pol with a seeded torch generator.
+    """
+    import torch
+    dev = torch.device(device)
+    T, B = uvw.shape[:2]
+    C = len(freq)
+    u = torch.as_tensor(uvw[..., 0].reshape(-1), device=dev, dtype=torch.float64)
+    v = torch.as_tensor(uvw[..., 1].reshape(-1), device=dev, dtype=torch.float64)
+    lt = torch.as_tensor(np.asarray(l), device=dev, dtype=torch.float64)
+    mt = torch.as_tensor(np.asarray(m), device=dev, dtype=torch.float64)
+    st = torch.as_tensor(np.asarray(flux), device=dev, dtype=torch.float32)
+    gen = torch.Generator(device=dev)
+    gen.manual_seed(int(seed))
+    vis = torch.empty((T * B, C, n_pol), dtype=torch.complex64, device=dev)
+    two_pi = 2.0 * np.pi
+    n_src = len(flux)
+    rows_per = max(1, (1 << 27) // max(n_src, 1))
+    for r0 in range(0, T * B, rows_per):
+        r1 = min(T * B, r0 + rows_per)
+        base = -(u[r0:r1, None] * lt[None, :] + v[r0:r1, None] * mt[None, :]) / C_LIGHT   # turns per Hz
+        for c in range(C):
+            turns = base * float(freq[c])
+            turns = turns - torch.round(turns)
+            ph = (turns * two_pi).float()
+            re = (torch.cos(ph) * st).sum(-1)
+            im = (torch.sin(ph) * st).sum(-1)
+            for p in range(n_pol):
+                vr = re
+                vi = im
+                if noise_sigma > 0:
+                    vr = vr + noise_sigma * torch.randn(r1 - r0, generator=gen, device=dev)
+                    vi = vi + noise_sigma * torch.randn(r1 - r0, generator=gen, device=dev)
+                vis[r0:r1, c, p] = torch.complex(vr, vi)
+    return vis.view(T, B, C, n_pol)
+
+
 class Observation(dict):
     """Plain container for a synthetic observation (arrays + imaging parms)."""
     __getattr__ = dict.__getitem__
@@ -154,21 +195,33 @@ def make_observation(n_ant, layout, radius_m, n_time, dt_s, freq, n_pol, n_src,
     l, m = r * np.cos(th), r * np.sin(th)
     obs = Observation(uvw=uvw, freq=np.asarray(freq, dtype=np.float64), l=l, m=m, flux=flux,
                       enu=enu, image_size=list(image_size), cell_arcsec=list(cell_arcsec))
-    weight = np.ones((T, B, C, n_pol), dtype=np.float32)
+    weight = None
     flag = None
-    if flag_fraction > 0:
-        flag = rng.random((T, B, C, n_pol)) < flag_fraction
+    if vis_device is None:
+        weight = np.ones((T, B, C, n_pol), dtype=np.float32)
+        if flag_fraction > 0:
+            flag = rng.random((T, B, C, n_pol)) < flag_fraction
     obs['weight'] = weight
     obs['flag'] = flag
-    if with_vis:
-        vis = point_source_vis(uvw, obs['freq'], l, m, flux, n_pol, noise_sigma, rng, device=vis_device)
+    if with_vis and vis_device is None:
+        vis = point_source_vis(uvw, obs['freq'], l, m, flux, n_pol, noise_sigma, rng)
         if flag is not None:
-            if vis_device is None:
-                vis[flag] = np.nan
-            else:
-                import torch
-                vis[torch.as_tensor(flag, device=vis.device)] = complex('nan')
+            vis[flag] = np.nan
+            weight[flag] = np.nan
         obs['vis'] = vis
+    elif with_vis:
+        import torch
+        vis = point_source_vis_torch(uvw, obs['freq'], l, m, flux, n_pol, noise_sigma, seed + 1000, vis_device)
+        w = torch.ones((T, B, C, n_pol), dtype=torch.float32, device=vis_device)
+        if flag_fraction > 0:
+            gen = torch.Generator(device=vis_device)
+            gen.manual_seed(seed + 2000)
+            fl = torch.rand((T, B, C, n_pol), generator=gen, device=vis_device) < flag_fraction
+            vis[fl] = complex('nan')
+            w[fl] = float('nan')
+            del fl
+        obs['vis'] = vis
+        obs['weight'] = w
     return obs
 
 

@@ -197,6 +197,12 @@ int ngg_fft_correct_adjoint(const void *image, int image_is_f64, int64_t n_chan_
                             const double *sum_weight, const double *correction, void *grid,
                             void *stream);
 
+/* Profiling: when enabled, ngg_grid_ps records CUDA events on its stream
+ * around its binning phase and its tile-accumulation kernels. ngg_last_phase_ms
+ * waits for the last call's events and returns the two durations (ms). */
+void ngg_set_profiling(int enable);
+int ngg_last_phase_ms(double *binning_ms, double *tiles_ms);
+
 /* Release cached cuFFT plans and scratch held by the library. */
 void ngg_release_cache(void);
 

@@ -44,7 +44,7 @@ constexpr int TV = 64;      // tile columns (v, contiguous)
 constexpr int CH = 32;      // time steps per chunk
 constexpr int NW = 8;       // warps per CTA
 constexpr int NG = 8;       // track processors per warp (4 lanes each)
-constexpr int ROUND = 16;   // producer round length (steps)
+constexpr int ROUND = 8;    // producer round length (steps)
 constexpr int SUP = 7;
 constexpr int SC = 3;
 constexpr int MAX_TAB = 4096;
@@ -65,7 +65,10 @@ struct TileArgs {
     const int64_t *bin_start; // [n_bins + 1]
     void *grid;
     double *sum_weight;
-    int *work_counter;
+    int *work_counter;        // [0] tile queue, [1] zero queue
+    const int *bbox;          // busy tile range (tu0, tu1, tv0, tv1) over all image channels
+    const struct SubItem *subs;  // tile work items
+    const int *n_subs;        // number of tile work items (device)
     int64_t T, B, C, P;
     int64_t nu, nv;
     int n_img, ntu, ntv, nk;
@@ -74,6 +77,7 @@ struct TileArgs {
     int tab_len;       // floats in the table
     int tab_bytes;     // padded to 16
     int continuum;
+    unsigned bnk;      // n_baseline * n_chunks_per_track (32-bit chunk decode)
 };
 
 __global__ void k_chan(const double *freq, int C, double dl0, double dl1, int64_t nu, int64_t nv,
@@ -174,6 +178,20 @@ __global__ void k_emit(const float4 *bbox, const ChanParms *chan, int64_t C, int
         }
 }
 
+__global__ void k_bbox_init(int *bb) {
+    bb[0] = 0x7fffffff; bb[1] = -1; bb[2] = 0x7fffffff; bb[3] = -1;
+}
+
+// range of tiles holding any chunk, over all image channels
+__global__ void k_bbox(const int64_t *bin_start, int64_t n_bins, int64_t NT, int ntv, int *bb) {
+    const int64_t bin = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (bin >= n_bins || bin_start[bin] == bin_start[bin + 1]) return;
+    const int64_t tile = bin % NT;
+    const int tu = (int)(tile / ntv), tv = (int)(tile % ntv);
+    atomicMin(&bb[0], tu); atomicMax(&bb[1], tu);
+    atomicMin(&bb[2], tv); atomicMax(&bb[3], tv);
+}
+
 __global__ void k_bounds(const unsigned long long *keys, int64_t n, int64_t n_bins, int64_t *bin_start) {
     int64_t bin = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
     if (bin > n_bins) return;
@@ -188,14 +206,16 @@ __global__ void k_bounds(const unsigned long long *keys, int64_t n, int64_t n_bi
 
 // ---- the tile kernel -------------------------------------------------------
 
-template <int NP, bool CPLX>
-struct Acc;  // per-pol accumulator element
-template <int NP>
-struct Acc<NP, true> { float2 v[NP]; };
-template <int NP>
-struct Acc<NP, false> { float v[NP]; };
+constexpr int MAXE = 2048;   // chunk entries per tile work item; heavier bins are split
 
-__device__ __forceinline__ int mod7(int x) {  // x in [-20, 20] -> [0,7)
+struct SubItem {
+    int box_item;   // index of (tile in busy box, image channel)
+    int sub;        // part of the bin's entries
+    int nsub;       // parts of this bin (> 1: flush with atomics into a zeroed tile)
+    int pad;
+};
+
+__device__ __forceinline__ int mod7(int x) {
     int r = x % 7;
     return r < 0 ? r + 7 : r;
 }
@@ -215,22 +235,115 @@ __device__ __forceinline__ bool mbar_wait(unsigned addr, unsigned phase) {
     return false;
 }
 
+// box item -> (tile index, image channel, bin)
+struct BoxMap {
+    int bt0, bv0, nbu, nbv, n_img;
+    int64_t NT;
+    int ntv;
+    __device__ __forceinline__ void map(int64_t item, int &tiu, int &tiv, int &cimg, int64_t &bin) const {
+        const int64_t tix = item / n_img;
+        cimg = (int)(item % n_img);
+        tiu = bt0 + (int)(tix / nbv);
+        tiv = bv0 + (int)(tix % nbv);
+        bin = (int64_t)cimg * NT + (int64_t)tiu * ntv + tiv;
+    }
+};
+
+__device__ __forceinline__ BoxMap box_map(const int *bbox, int n_img, int64_t NT, int ntv) {
+    BoxMap m;
+    const bool have = bbox[0] <= bbox[1] && bbox[2] <= bbox[3];
+    m.bt0 = bbox[0];
+    m.bv0 = bbox[2];
+    m.nbu = have ? bbox[1] - bbox[0] + 1 : 0;
+    m.nbv = have ? bbox[3] - bbox[2] + 1 : 0;
+    m.n_img = n_img;
+    m.NT = NT;
+    m.ntv = ntv;
+    return m;
+}
+
+// number of work items of every box item (0 beyond the box)
+__global__ void k_nsub(const int64_t *bin_start, const int *bbox, int n_img, int64_t NT, int ntv, int64_t n_bound,
+                       int *nsub) {
+    const int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (i > n_bound) return;
+    const BoxMap m = box_map(bbox, n_img, NT, ntv);
+    const int64_t n_box = (int64_t)m.nbu * m.nbv * n_img;
+    int k = 0;
+    if (i < n_box) {
+        int tiu, tiv, cimg;
+        int64_t bin;
+        m.map(i, tiu, tiv, cimg, bin);
+        const int64_t n = bin_start[bin + 1] - bin_start[bin];
+        k = n > MAXE ? (int)((n + MAXE - 1) / MAXE) : 1;
+    }
+    nsub[i] = k;
+}
+
+__global__ void k_fill_subs(const int *nsub, const int *off, int64_t n_bound, SubItem *subs, int *n_total) {
+    const int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= n_bound) return;
+    const int k = nsub[i], o = off[i];
+    for (int s = 0; s < k; ++s) subs[o + s] = SubItem{(int)i, s, k, 0};
+    if (i == n_bound - 1) *n_total = o + k;
+}
+
+// zero the destination of bins split over several work items (they add
+// their partial tiles with atomics)
+template <bool CPLX, bool FFTL>
+__global__ void k_zero_split(const int64_t *bin_start, const int *bbox, int n_img, int64_t NT, int ntv,
+                             int64_t n_bound, void *grid, int64_t P, int p0, int np, int64_t nu, int64_t nv) {
+    const int64_t i = blockIdx.x;
+    if (i >= n_bound) return;
+    const BoxMap m = box_map(bbox, n_img, NT, ntv);
+    if (i >= (int64_t)m.nbu * m.nbv * n_img) return;
+    int tiu, tiv, cimg;
+    int64_t bin;
+    m.map(i, tiu, tiv, cimg, bin);
+    if (bin_start[bin + 1] - bin_start[bin] <= MAXE) return;
+    const int u0 = tiu * TU, v0 = tiv * TV;
+    const int cu_c = (int)(nu / 2), cv_c = (int)(nv / 2);
+    for (int e = threadIdx.x; e < np * TU * TV; e += blockDim.x) {
+        const int p = e / (TU * TV), r = (e / TV) % TU, cl = e % TV;
+        int u = u0 + r, v = v0 + cl;
+        if (u >= nu || v >= nv) continue;
+        if (FFTL) {
+            u = u < cu_c ? u + (int)(nu - cu_c) : u - cu_c;
+            v = v < cv_c ? v + (int)(nv - cv_c) : v - cv_c;
+        }
+        const int64_t off = (((int64_t)cimg * P + p0 + p) * nu + u) * nv + v;
+        if (CPLX || FFTL) reinterpret_cast<float2 *>(grid)[off] = make_float2(0.f, 0.f);
+        else reinterpret_cast<float *>(grid)[off] = 0.f;
+    }
+}
+
+// register accumulator of one (column, row) cell
+template <bool CPLX>
+struct Cell;
+template <>
+struct Cell<true> { float2 a, b; };   // (re, im) of pol 0 and pol 1
+template <>
+struct Cell<false> { float2 a; };     // (pol 0, pol 1) of a real grid
+
 template <int NP, bool CPLX, bool FFTL>
 __global__ void __launch_bounds__(NW * 32, 2) k_tiles(const TileArgs a) {
     extern __shared__ __align__(16) unsigned char smem[];
-    // layout: acc tile | table | norm sums | records | misc
+    // layout: acc tile | table | norm sums | records | group info | misc
     constexpr int ACC_ELEM = CPLX ? 8 : 4;
+    constexpr int NREC = NG * ROUND;   // records per warp
     float *acc_s = reinterpret_cast<float *>(smem);
     const size_t acc_bytes = (size_t)NP * TU * TV * ACC_ELEM;
     float *tab = reinterpret_cast<float *>(smem + acc_bytes);
     float *nsum = tab + ((a.tab_bytes + 3) / 4);
     const int nsum_len = a.os + 1;
-    unsigned *rec_cuv = reinterpret_cast<unsigned *>(nsum + ((nsum_len + 3) & ~3));
-    int *rec_info = reinterpret_cast<int *>(rec_cuv + NW * NG * ROUND);
-    float4 *rec_wv = reinterpret_cast<float4 *>(rec_info + NW * NG * ROUND);
-    double *sw_part = reinterpret_cast<double *>(rec_wv + NW * NG * ROUND);
+    float4 *rec_wv = reinterpret_cast<float4 *>(nsum + ((nsum_len + 3) & ~3));
+    float4 *rec_tv = rec_wv + NW * NREC;              // 2 per record
+    unsigned *rec_cuv = reinterpret_cast<unsigned *>(rec_tv + 2 * NW * NREC);
+    int *rec_info = reinterpret_cast<int *>(rec_cuv + NW * NREC);
+    int4 *ginfo = reinterpret_cast<int4 *>(rec_info + NW * NREC);   // (c, b, t0, valid) per group
+    double *sw_part = reinterpret_cast<double *>(ginfo + NW * NG);
     unsigned long long *mbar = reinterpret_cast<unsigned long long *>(sw_part + NW * 4);
-    int *s_item = reinterpret_cast<int *>(mbar + 1);
+    int *s_item = reinterpret_cast<int *>(mbar + 1);   // [kind, item]
 
     const int tid = threadIdx.x;
     const int warp = tid >> 5, lane = tid & 31;
@@ -251,45 +364,101 @@ __global__ void __launch_bounds__(NW * 32, 2) k_tiles(const TileArgs a) {
             "l"(a.tab_g), "r"(a.tab_bytes), "r"(mbar_addr)
             : "memory");
     }
-    bool tma_ok = mbar_wait(mbar_addr, 0);
-    if (!tma_ok) {  // bounded wait ran out: load the table with plain loads instead
+    const bool tma_ok = mbar_wait(mbar_addr, 0);
+    if (!tma_ok) {  // the bounded wait ran out: fall back to plain loads
         for (int i = tid; i < a.tab_len; i += blockDim.x) tab[i] = a.tab_g[i];
     }
     __syncthreads();
-    // norm sums: nsum[o + os/2] = sum_{i=-3..3} tab[|os*i + o|]
     const int half_os = a.os / 2;
-    for (int i = tid; i < nsum_len; i += blockDim.x) {
-        int o = i - half_os;
+    for (int i = tid; i < nsum_len; i += blockDim.x) {   // nsum[o+os/2] = sum_i tab[|os*i+o|]
+        const int o = i - half_os;
         float s = 0.f;
         for (int d = -SC; d <= SC; ++d) {
-            int ix = abs(a.os * d + o);
+            const int ix = abs(a.os * d + o);
             s += ix < a.tab_len ? tab[ix] : 0.f;
         }
         nsum[i] = s;
     }
-    // zero the accumulator tile
     for (int i = tid; i < NP * TU * TV * (CPLX ? 2 : 1); i += blockDim.x) acc_s[i] = 0.f;
     __syncthreads();
 
     const int64_t NT = (int64_t)a.ntu * a.ntv;
-    const int64_t n_items = NT * a.n_img;
     const int cu_c = (int)(a.nu / 2), cv_c = (int)(a.nv / 2);
-    const int g = lane >> 2;          // track processor in the warp
-    const int l4 = lane & 3;          // lane within the processor
+    const int g = lane >> 2;            // track processor in the warp
+    const int l4 = lane & 3;            // lane within the processor
     const int ncol = (l4 < 3) ? 2 : 1;  // column classes l4 and l4+4
+    const int64_t plane = a.nu * a.nv;
+    const BoxMap bm = box_map(a.bbox, a.n_img, NT, a.ntv);
+    const int R0 = bm.nbu ? bm.bt0 * TU : 0, R1 = bm.nbu ? min((bm.bt0 + bm.nbu) * TU, (int)a.nu) : 0;
+    const int V0 = bm.nbv ? bm.bv0 * TV : 0, V1 = bm.nbv ? min((bm.bv0 + bm.nbv) * TV, (int)a.nv) : 0;
+    const int64_t n_tile_items = *a.n_subs;
+    constexpr int ZR = 8;
+    const int nrb = (int)((a.nu + ZR - 1) / ZR);
+    const int64_t n_zero_items = (int64_t)a.n_img * NP * nrb;
+    const int order0 = blockIdx.x & 1;   // odd CTAs start with zero rows
+    int stage = 0;
+
+    int4 *my_ginfo = ginfo + warp * NG;
+    unsigned *my_cuv = rec_cuv + warp * NREC;
+    int *my_info = rec_info + warp * NREC;
+    float4 *my_wv = rec_wv + warp * NREC;
+    float4 *my_tv = rec_tv + 2 * warp * NREC;
 
     for (;;) {
-        if (tid == 0) *s_item = atomicAdd(a.work_counter, 1);
+        if (tid == 0) {
+            int kind = -1;
+            long long it = 0;
+            while (stage < 2) {
+                const int which = stage == 0 ? order0 : 1 - order0;
+                if (which == 0) {
+                    it = atomicAdd(&a.work_counter[0], 1);
+                    if (it < n_tile_items) { kind = 0; break; }
+                } else {
+                    it = atomicAdd(&a.work_counter[1], 1);
+                    if (it < n_zero_items) { kind = 1; break; }
+                }
+                ++stage;
+            }
+            s_item[0] = kind;
+            s_item[1] = (int)it;
+        }
         __syncthreads();
-        const int64_t item = *s_item;
-        if (item >= n_items) break;
-        const int64_t tile = item / a.n_img;
-        const int cimg = (int)(item % a.n_img);
-        const int tiu = (int)(tile / a.ntv), tiv = (int)(tile % a.ntv);
+        const int kind = s_item[0];
+        const int64_t item = s_item[1];
+        if (kind < 0) break;
+        if (kind == 1) {
+            // ---------------- zero rows outside the busy box ----------------
+            const int64_t q = item / nrb;
+            const int rb = (int)(item % nrb);
+            const int cimg = (int)(q / NP), p = (int)(q % NP);
+            const int64_t pbase = ((int64_t)cimg * a.P + a.p0 + p) * plane;
+            const int r_end = min(rb * ZR + ZR, (int)a.nu);
+            for (int r = rb * ZR; r < r_end; ++r) {
+                int un = r;
+                if (FFTL) un = r + cu_c >= a.nu ? r + cu_c - (int)a.nu : r + cu_c;   // natural row
+                const bool in_band = un >= R0 && un < R1;
+                for (int dv = tid; dv < a.nv; dv += blockDim.x) {
+                    int vn = dv;
+                    if (FFTL) vn = dv + cv_c >= a.nv ? dv + cv_c - (int)a.nv : dv + cv_c;
+                    if (!in_band || vn < V0 || vn >= V1) {
+                        const int64_t off = pbase + (int64_t)r * a.nv + dv;
+                        if (CPLX || FFTL) reinterpret_cast<float2 *>(a.grid)[off] = make_float2(0.f, 0.f);
+                        else reinterpret_cast<float *>(a.grid)[off] = 0.f;
+                    }
+                }
+            }
+            __syncthreads();
+            continue;
+        }
+        const SubItem si = a.subs[item];
+        int tiu, tiv, cimg;
+        int64_t bin;
+        bm.map(si.box_item, tiu, tiv, cimg, bin);
         const int u0 = tiu * TU, v0 = tiv * TV;
-        const int64_t bin = (int64_t)cimg * NT + tile;
-        const int64_t e0 = a.bin_start[bin], e1 = a.bin_start[bin + 1];
-        const int64_t plane = a.nu * a.nv;
+        const int64_t b0 = a.bin_start[bin], b1 = a.bin_start[bin + 1];
+        const int64_t e0 = b0 + ((b1 - b0) * si.sub) / si.nsub;
+        const int64_t e1 = b0 + ((b1 - b0) * (si.sub + 1)) / si.nsub;
+        const bool split = si.nsub > 1;
 
         if (e0 < e1) {
             // ---------------- busy tile ----------------
@@ -299,136 +468,136 @@ __global__ void __launch_bounds__(NW * 32, 2) k_tiles(const TileArgs a) {
             const int64_t re = e0 + (n * (gi + 1)) / (NW * NG);
             int jmax = (int)(re - rs);
             for (int o = 16; o > 0; o >>= 1) jmax = max(jmax, __shfl_xor_sync(0xffffffffu, jmax, o));
-            // producer ranges for the groups this lane produces for
             float sw_s[NP], sw_c[NP];
 #pragma unroll
             for (int p = 0; p < NP; ++p) { sw_s[p] = 0.f; sw_c[p] = 0.f; }
-            // consumer state
             int prev_cu = -(1 << 28), prev_cv = -(1 << 28);
             int col[2] = {-(1 << 28), -(1 << 28)};
             bool colv[2] = {false, false};
-            Acc<NP, CPLX> acc[2][SUP];
+            Cell<CPLX> acc[2][SUP];
 #pragma unroll
             for (int j = 0; j < 2; ++j)
 #pragma unroll
-                for (int d = 0; d < SUP; ++d)
-#pragma unroll
-                    for (int p = 0; p < NP; ++p) {
-                        if constexpr (CPLX) acc[j][d].v[p] = make_float2(0.f, 0.f);
-                        else acc[j][d].v[p] = 0.f;
-                    }
+                for (int d = 0; d < SUP; ++d) {
+                    acc[j][d].a = make_float2(0.f, 0.f);
+                    if constexpr (CPLX) acc[j][d].b = make_float2(0.f, 0.f);
+                }
 
             auto flush_cell = [&](int j, int d) {
-                int row = prev_cv - SC + d;
+                const int row = prev_cv - SC + d;
                 if (!colv[j] || row < v0 || row >= v0 + TV || row >= a.nv) return;
-                int lu = col[j] - u0, lv = row - v0;
-#pragma unroll
-                for (int p = 0; p < NP; ++p) {
-                    if constexpr (CPLX) {
-                        float2 x = acc[j][d].v[p];
-                        if (x.x != 0.f || x.y != 0.f) {
-                            float *q = acc_s + 2 * (((size_t)p * TU + lu) * TV + lv);
-                            atomicAdd(q, x.x);
-                            atomicAdd(q + 1, x.y);
-                        }
-                    } else {
-                        float x = acc[j][d].v[p];
-                        if (x != 0.f) atomicAdd(acc_s + ((size_t)p * TU + lu) * TV + lv, x);
+                const int lu = col[j] - u0, lv = row - v0;
+                if constexpr (CPLX) {
+                    const float2 x = acc[j][d].a;
+                    if (x.x != 0.f || x.y != 0.f) {
+                        float *q = acc_s + 2 * ((size_t)lu * TV + lv);
+                        atomicAdd(q, x.x);
+                        atomicAdd(q + 1, x.y);
                     }
+                    if (NP > 1) {
+                        const float2 y = acc[j][d].b;
+                        if (y.x != 0.f || y.y != 0.f) {
+                            float *q = acc_s + 2 * (((size_t)TU + lu) * TV + lv);
+                            atomicAdd(q, y.x);
+                            atomicAdd(q + 1, y.y);
+                        }
+                    }
+                } else {
+                    const float2 x = acc[j][d].a;
+                    if (x.x != 0.f) atomicAdd(acc_s + (size_t)lu * TV + lv, x.x);
+                    if (NP > 1 && x.y != 0.f) atomicAdd(acc_s + ((size_t)TU + lu) * TV + lv, x.y);
                 }
             };
             auto zero_cell = [&](int j, int d) {
-#pragma unroll
-                for (int p = 0; p < NP; ++p) {
-                    if constexpr (CPLX) acc[j][d].v[p] = make_float2(0.f, 0.f);
-                    else acc[j][d].v[p] = 0.f;
-                }
+                acc[j][d].a = make_float2(0.f, 0.f);
+                if constexpr (CPLX) acc[j][d].b = make_float2(0.f, 0.f);
             };
 
-            unsigned *my_cuv = rec_cuv + warp * NG * ROUND;
-            int *my_info = rec_info + warp * NG * ROUND;
-            float4 *my_wv = rec_wv + warp * NG * ROUND;
-
             for (int j = 0; j < jmax; ++j) {
-                // decode the chunk of every group for the producer side
+                // decode the chunk of each group once
+                if (lane < NG) {
+                    const int ggi = warp * NG + lane;
+                    const int64_t grs = e0 + (n * ggi) / (NW * NG);
+                    const int64_t gre = e0 + (n * (ggi + 1)) / (NW * NG);
+                    int4 gi4 = make_int4(0, 0, 0, 0);
+                    if (grs + j < gre) {
+                        const unsigned chu = (unsigned)(a.keys[grs + j] & 0xffffffffull);
+                        const unsigned cq = chu / a.bnk;
+                        const unsigned rem = chu - cq * a.bnk;
+                        const unsigned bq = rem / (unsigned)a.nk;
+                        gi4 = make_int4((int)cq, (int)bq, (int)((rem - bq * (unsigned)a.nk) * CH), 1);
+                    }
+                    my_ginfo[lane] = gi4;
+                }
+                __syncwarp();
                 for (int rnd = 0; rnd < CH / ROUND; ++rnd) {
-                    // ---- producer: 4 records per lane ----
+                    // ---- producer: 2 records per lane ----
 #pragma unroll
-                    for (int k4 = 0; k4 < 4; ++k4) {
-                        const int r = lane + 32 * k4;
+                    for (int k2 = 0; k2 < 2; ++k2) {
+                        const int r = lane + 32 * k2;
                         const int gg = r / ROUND, s = r % ROUND;
-                        const int ggi = warp * NG + gg;
-                        const int64_t grs = e0 + (n * ggi) / (NW * NG);
-                        const int64_t gre = e0 + (n * (ggi + 1)) / (NW * NG);
+                        const int4 gi4 = my_ginfo[gg];
                         unsigned cuv = 0;
                         int info = 0;
                         float4 wv = make_float4(0.f, 0.f, 0.f, 0.f);
-                        if (grs + j < gre) {
-                            const unsigned long long key = a.keys[grs + j];
-                            const int64_t ch = (int64_t)(key & 0xffffffffull);
-                            const int64_t c = ch / (a.B * a.nk);
-                            const int64_t b = (ch / a.nk) % a.B;
-                            const int64_t kk = ch % a.nk;
-                            const int64_t t = kk * CH + rnd * ROUND + s;
-                            if (t < a.T) {
-                                const float4 us = a.uvs[b * a.T + t];
-                                if (!isnan(us.x) && !isnan(us.z)) {
-                                    const ChanParms cp = a.chan[c];
-                                    int cu, ou, cv, ov;
-                                    if (!cell_pair(us.x, us.y, cp.suh, cp.sul, false, cu_c, a.os, cu, ou)) {
-                                        long long i64, o64;
-                                        cell_fp64(a.uvw[(t * a.B + b) * 3 + 0], cp.su, false, cu_c, a.os, i64, o64);
-                                        cu = (int)max(min(i64, (long long)1 << 30), -((long long)1 << 30));
-                                        ou = (int)o64;
-                                    }
-                                    if (!cell_pair(us.z, us.w, cp.svh, cp.svl, false, cv_c, a.os, cv, ov)) {
-                                        long long i64, o64;
-                                        cell_fp64(a.uvw[(t * a.B + b) * 3 + 1], cp.sv, false, cv_c, a.os, i64, o64);
-                                        cv = (int)max(min(i64, (long long)1 << 30), -((long long)1 << 30));
-                                        ov = (int)o64;
-                                    }
-                                    if (cu - SC >= 0 && cu + SC < a.nu && cv - SC >= 0 && cv + SC < a.nv) {
-                                        const int64_t base = ((t * a.B + b) * a.C + c) * a.P + a.p0;
-                                        float w[NP];
-                                        bool pv[NP];
-                                        bool any = false;
-                                        float val[2 * NP];
+                        float4 tva = make_float4(0.f, 0.f, 0.f, 0.f), tvb = tva;
+                        const int64_t t = (int64_t)gi4.z + rnd * ROUND + s;
+                        if (gi4.w && t < a.T) {
+                            const int64_t c = gi4.x, b = gi4.y;
+                            const float4 us = a.uvs[b * a.T + t];
+                            if (!isnan(us.x) && !isnan(us.z)) {
+                                const ChanParms cp = a.chan[c];
+                                int cu, ou, cv, ov;
+                                if (!cell_pair(us.x, us.y, cp.suh, cp.sul, false, cu_c, a.os, cu, ou)) {
+                                    long long i64, o64;
+                                    cell_fp64(a.uvw[(t * a.B + b) * 3 + 0], cp.su, false, cu_c, a.os, i64, o64);
+                                    cu = (int)max(min(i64, (long long)1 << 30), -((long long)1 << 30));
+                                    ou = (int)o64;
+                                }
+                                if (!cell_pair(us.z, us.w, cp.svh, cp.svl, false, cv_c, a.os, cv, ov)) {
+                                    long long i64, o64;
+                                    cell_fp64(a.uvw[(t * a.B + b) * 3 + 1], cp.sv, false, cv_c, a.os, i64, o64);
+                                    cv = (int)max(min(i64, (long long)1 << 30), -((long long)1 << 30));
+                                    ov = (int)o64;
+                                }
+                                if (cu - SC >= 0 && cu + SC < a.nu && cv - SC >= 0 && cv + SC < a.nv) {
+                                    const int64_t base = ((t * a.B + b) * a.C + c) * a.P + a.p0;
+                                    float w[NP];
+                                    bool pv[NP];
+                                    bool any = false;
 #pragma unroll
-                                        for (int p = 0; p < NP; ++p) {
-                                            w[p] = a.weight[base + p];
-                                            if constexpr (CPLX) {
-                                                const float2 vv = a.vis[base + p];
-                                                float xr = vv.x * w[p], xi = vv.y * w[p];
-                                                pv[p] = !isnan(xr) && !isnan(xi) && (xr != 0.f || xi != 0.f);
-                                                val[2 * p] = pv[p] ? xr : 0.f;
-                                                val[2 * p + 1] = pv[p] ? xi : 0.f;
-                                            } else {
-                                                pv[p] = !isnan(w[p]) && w[p] != 0.f;
-                                                val[p] = pv[p] ? w[p] : 0.f;
-                                            }
-                                            any = any || pv[p];
+                                    for (int p = 0; p < NP; ++p) {
+                                        w[p] = a.weight[base + p];
+                                        if constexpr (CPLX) {
+                                            const float2 vv = a.vis[base + p];
+                                            const float xr = vv.x * w[p], xi = vv.y * w[p];
+                                            pv[p] = !isnan(xr) && !isnan(xi) && (xr != 0.f || xi != 0.f);
+                                            if (p == 0) { wv.x = pv[p] ? xr : 0.f; wv.y = pv[p] ? xi : 0.f; }
+                                            else { wv.z = pv[p] ? xr : 0.f; wv.w = pv[p] ? xi : 0.f; }
+                                        } else {
+                                            pv[p] = !isnan(w[p]) && w[p] != 0.f;
+                                            if (p == 0) wv.x = pv[p] ? w[p] : 0.f;
+                                            else wv.y = pv[p] ? w[p] : 0.f;
                                         }
-                                        if (any) {
-                                            if constexpr (CPLX) {
-                                                wv.x = val[0]; wv.y = val[1];
-                                                if (NP > 1) { wv.z = val[2 * (NP - 1)]; wv.w = val[2 * (NP - 1) + 1]; }
-                                            } else {
-                                                wv.x = val[0];
-                                                if (NP > 1) wv.y = val[NP - 1];
-                                            }
-                                            cuv = ((unsigned)cu << 16) | (unsigned)cv;
-                                            info = 1 | ((ou + 1024) << 1) | ((ov + 1024) << 12);
-                                            // sum of weights: home tile only
-                                            if (cu >= u0 && cu < u0 + TU && cv >= v0 && cv < v0 + TV) {
-                                                const float norm = nsum[ou + half_os] * nsum[ov + half_os];
+                                        any = any || pv[p];
+                                    }
+                                    if (any) {
+                                        cuv = ((unsigned)cu << 16) | (unsigned)cv;
+                                        info = 1 | ((ou + 1024) << 1);
+                                        float tv[SUP];
 #pragma unroll
-                                                for (int p = 0; p < NP; ++p) {
-                                                    if (pv[p]) {  // Kahan
-                                                        float y = __fsub_rn(__fmul_rn(w[p], norm), sw_c[p]);
-                                                        float tt = __fadd_rn(sw_s[p], y);
-                                                        sw_c[p] = __fsub_rn(__fsub_rn(tt, sw_s[p]), y);
-                                                        sw_s[p] = tt;
-                                                    }
+                                        for (int d = 0; d < SUP; ++d) tv[d] = tab[abs(a.os * (d - SC) + ov)];
+                                        tva = make_float4(tv[0], tv[1], tv[2], tv[3]);
+                                        tvb = make_float4(tv[4], tv[5], tv[6], 0.f);
+                                        if (cu >= u0 && cu < u0 + TU && cv >= v0 && cv < v0 + TV) {
+                                            const float norm = nsum[ou + half_os] * nsum[ov + half_os];
+#pragma unroll
+                                            for (int p = 0; p < NP; ++p) {
+                                                if (pv[p]) {  // Kahan
+                                                    const float y = __fsub_rn(__fmul_rn(w[p], norm), sw_c[p]);
+                                                    const float tt = __fadd_rn(sw_s[p], y);
+                                                    sw_c[p] = __fsub_rn(__fsub_rn(tt, sw_s[p]), y);
+                                                    sw_s[p] = tt;
                                                 }
                                             }
                                         }
@@ -436,26 +605,27 @@ __global__ void __launch_bounds__(NW * 32, 2) k_tiles(const TileArgs a) {
                                 }
                             }
                         }
-                        my_cuv[gg * ROUND + s] = cuv;
-                        my_info[gg * ROUND + s] = info;
-                        my_wv[gg * ROUND + s] = wv;
+                        const int ri = gg * ROUND + s;
+                        my_cuv[ri] = cuv;
+                        my_info[ri] = info;
+                        my_wv[ri] = wv;
+                        my_tv[2 * ri] = tva;
+                        my_tv[2 * ri + 1] = tvb;
                     }
                     __syncwarp();
-                    // ---- consumer: 16 steps of this processor's chunk ----
+                    // ---- consumer: ROUND steps of this processor's chunk ----
                     for (int s = 0; s < ROUND; ++s) {
-                        const int info = my_info[g * ROUND + s];
+                        const int ri = g * ROUND + s;
+                        const int info = my_info[ri];
                         if (!(info & 1)) continue;
-                        const unsigned cuv = my_cuv[g * ROUND + s];
-                        const float4 wv = my_wv[g * ROUND + s];
+                        const unsigned cuv = my_cuv[ri];
                         const int cu = (int)(cuv >> 16), cv = (int)(cuv & 0xffffu);
                         const int ou = ((info >> 1) & 2047) - 1024;
-                        const int ov = ((info >> 12) & 2047) - 1024;
                         if (cu != prev_cu) {
 #pragma unroll
                             for (int jj = 0; jj < 2; ++jj) {
                                 if (jj < ncol) {
-                                    const int acls = l4 + 4 * jj;
-                                    const int nc = cu - SC + mod7(acls - (cu - SC));
+                                    const int nc = cu - SC + mod7(l4 + 4 * jj - (cu - SC));
                                     if (nc != col[jj]) {
 #pragma unroll
                                         for (int d = 0; d < SUP; ++d) { flush_cell(jj, d); zero_cell(jj, d); }
@@ -475,7 +645,7 @@ __global__ void __launch_bounds__(NW * 32, 2) k_tiles(const TileArgs a) {
                                     for (int d = 0; d < SUP; ++d) { flush_cell(jj, d); zero_cell(jj, d); }
                                 prev_cv = cv;
                             } else {
-                                while (delta > 0) {  // window moves to larger v
+                                while (delta > 0) {
 #pragma unroll
                                     for (int jj = 0; jj < 2; ++jj) {
                                         flush_cell(jj, 0);
@@ -499,33 +669,27 @@ __global__ void __launch_bounds__(NW * 32, 2) k_tiles(const TileArgs a) {
                                 }
                             }
                         }
-                        // taps
-                        float tv[SUP];
-#pragma unroll
-                        for (int d = 0; d < SUP; ++d) tv[d] = tab[abs(a.os * (d - SC) + ov)];
+                        const float4 wv = my_wv[ri];
+                        const float4 tva = my_tv[2 * ri], tvb = my_tv[2 * ri + 1];
+                        const float tv[SUP] = {tva.x, tva.y, tva.z, tva.w, tvb.x, tvb.y, tvb.z};
 #pragma unroll
                         for (int jj = 0; jj < 2; ++jj) {
                             if (jj < ncol) {
                                 const float tu = tab[abs(a.os * (col[jj] - cu) + ou)];
+                                const float2 tu2 = make_float2(tu, tu);
+                                const float2 A0 = __fmul2_rn(tu2, make_float2(wv.x, wv.y));
                                 if constexpr (CPLX) {
-                                    const float2 A0 = make_float2(tu * wv.x, tu * wv.y);
-                                    const float2 A1 = make_float2(tu * wv.z, tu * wv.w);
+                                    const float2 A1 = __fmul2_rn(tu2, make_float2(wv.z, wv.w));
 #pragma unroll
                                     for (int d = 0; d < SUP; ++d) {
-                                        acc[jj][d].v[0].x = fmaf(A0.x, tv[d], acc[jj][d].v[0].x);
-                                        acc[jj][d].v[0].y = fmaf(A0.y, tv[d], acc[jj][d].v[0].y);
-                                        if (NP > 1) {
-                                            acc[jj][d].v[NP - 1].x = fmaf(A1.x, tv[d], acc[jj][d].v[NP - 1].x);
-                                            acc[jj][d].v[NP - 1].y = fmaf(A1.y, tv[d], acc[jj][d].v[NP - 1].y);
-                                        }
+                                        const float2 t2 = make_float2(tv[d], tv[d]);
+                                        acc[jj][d].a = __ffma2_rn(A0, t2, acc[jj][d].a);
+                                        if (NP > 1) acc[jj][d].b = __ffma2_rn(A1, t2, acc[jj][d].b);
                                     }
                                 } else {
-                                    const float A0 = tu * wv.x, A1 = tu * wv.y;
 #pragma unroll
-                                    for (int d = 0; d < SUP; ++d) {
-                                        acc[jj][d].v[0] = fmaf(A0, tv[d], acc[jj][d].v[0]);
-                                        if (NP > 1) acc[jj][d].v[NP - 1] = fmaf(A1, tv[d], acc[jj][d].v[NP - 1]);
-                                    }
+                                    for (int d = 0; d < SUP; ++d)
+                                        acc[jj][d].a = __ffma2_rn(A0, make_float2(tv[d], tv[d]), acc[jj][d].a);
                                 }
                             }
                         }
@@ -533,12 +697,10 @@ __global__ void __launch_bounds__(NW * 32, 2) k_tiles(const TileArgs a) {
                     __syncwarp();
                 }
             }
-            // final flush of the register state
 #pragma unroll
             for (int jj = 0; jj < 2; ++jj)
 #pragma unroll
                 for (int d = 0; d < SUP; ++d) flush_cell(jj, d);
-            // sum of weights: lane -> warp -> CTA -> global
 #pragma unroll
             for (int p = 0; p < NP; ++p) {
                 double v = (double)sw_s[p] - (double)sw_c[p];
@@ -553,33 +715,46 @@ __global__ void __launch_bounds__(NW * 32, 2) k_tiles(const TileArgs a) {
             }
         }
 
-        // ---------------- write the tile (zeros if empty) ----------------
+        // ---------------- write the tile ----------------
         const bool busy = e0 < e1;
-        for (int e = tid; e < NP * TU * TV; e += blockDim.x) {
-            const int p = e / (TU * TV);
-            const int r = (e / TV) % TU;
-            const int cl = e % TV;
-            const int u = u0 + r, v = v0 + cl;
-            float2 val = make_float2(0.f, 0.f);
-            if (busy) {
-                if constexpr (CPLX) {
-                    float2 *q = reinterpret_cast<float2 *>(acc_s) + e;
-                    val = *q;
-                    *q = make_float2(0.f, 0.f);
-                } else {
-                    val.x = acc_s[e];
-                    acc_s[e] = 0.f;
+        if (!(split && !busy)) {
+            for (int e = tid; e < NP * TU * TV; e += blockDim.x) {
+                const int p = e / (TU * TV);
+                const int r = (e / TV) % TU;
+                const int cl = e % TV;
+                const int u = u0 + r, v = v0 + cl;
+                float2 val = make_float2(0.f, 0.f);
+                if (busy) {
+                    if constexpr (CPLX) {
+                        float2 *q = reinterpret_cast<float2 *>(acc_s) + e;
+                        val = *q;
+                        *q = make_float2(0.f, 0.f);
+                    } else {
+                        val.x = acc_s[e];
+                        acc_s[e] = 0.f;
+                    }
                 }
-            }
-            if (u < a.nu && v < a.nv) {
-                int64_t du = u, dv = v;
-                if (FFTL) {  // (x - N/2) mod N for x in [0, N)
-                    du = u < cu_c ? u + (a.nu - cu_c) : u - cu_c;
-                    dv = v < cv_c ? v + (a.nv - cv_c) : v - cv_c;
+                if (u < a.nu && v < a.nv) {
+                    int du = u, dv = v;
+                    if (FFTL) {  // (x - N/2) mod N for x in [0, N)
+                        du = u < cu_c ? u + ((int)a.nu - cu_c) : u - cu_c;
+                        dv = v < cv_c ? v + ((int)a.nv - cv_c) : v - cv_c;
+                    }
+                    const int64_t off = ((int64_t)cimg * a.P + a.p0 + p) * plane + (int64_t)du * a.nv + dv;
+                    if (split) {
+                        if (CPLX || FFTL) {
+                            float *q = reinterpret_cast<float *>(reinterpret_cast<float2 *>(a.grid) + off);
+                            if (val.x != 0.f) atomicAdd(q, val.x);
+                            if (val.y != 0.f) atomicAdd(q + 1, val.y);
+                        } else if (val.x != 0.f) {
+                            atomicAdd(reinterpret_cast<float *>(a.grid) + off, val.x);
+                        }
+                    } else if (CPLX || FFTL) {
+                        reinterpret_cast<float2 *>(a.grid)[off] = val;
+                    } else {
+                        reinterpret_cast<float *>(a.grid)[off] = val.x;
+                    }
                 }
-                const int64_t off = ((int64_t)cimg * a.P + a.p0 + p) * plane + du * a.nv + dv;
-                if (CPLX || FFTL) reinterpret_cast<float2 *>(a.grid)[off] = val;
-                else reinterpret_cast<float *>(a.grid)[off] = val.x;
             }
         }
         __syncthreads();
@@ -590,29 +765,36 @@ size_t tile_smem_bytes(int np, bool cplx, int tab_bytes, int os) {
     size_t acc = (size_t)np * TU * TV * (cplx ? 8 : 4);
     size_t tab = (size_t)((tab_bytes + 3) / 4) * 4;
     size_t ns = (size_t)(((os + 1) + 3) & ~3) * 4;
-    size_t rec = (size_t)NW * NG * ROUND * (4 + 4 + 16);
+    size_t rec = (size_t)NW * NG * ROUND * (16 + 32 + 4 + 4);
+    size_t gin = (size_t)NW * NG * 16;
     size_t misc = NW * 4 * 8 + 8 + 16;
-    return acc + tab + ns + rec + misc;
+    return acc + tab + ns + rec + gin + misc;
 }
 
 template <int NP, bool CPLX, bool FFTL>
-int launch_tiles(const TileArgs &ta, cudaStream_t s) {
+int launch_tiles(const TileArgs &ta, int64_t n_bound, cudaStream_t s) {
     size_t smem = tile_smem_bytes(NP, CPLX, ta.tab_bytes, ta.os);
     auto kern = k_tiles<NP, CPLX, FFTL>;
     NGG_CUDA(cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
     int per_sm = 0;
     NGG_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, kern, NW * 32, smem));
     if (per_sm < 1) return fail(NGG_ERR_UNSUPPORTED, "k_tiles does not fit on an SM");
-    int grid = num_sms() * per_sm;
+    if (n_bound > 0) {
+        k_zero_split<CPLX, FFTL><<<(unsigned)n_bound, 256, 0, s>>>(ta.bin_start, ta.bbox, ta.n_img,
+                                                                    (int64_t)ta.ntu * ta.ntv, ta.ntv, n_bound,
+                                                                    ta.grid, ta.P, ta.p0, NP, ta.nu, ta.nv);
+        NGG_CHECK_LAUNCH("k_zero_split");
+    }
+    const int grid = num_sms() * per_sm;
     kern<<<grid, NW * 32, smem, s>>>(ta);
     NGG_CHECK_LAUNCH("k_tiles");
     return NGG_OK;
 }
 
 template <int NP>
-int dispatch_tiles(const TileArgs &ta, bool cplx, bool fftl, cudaStream_t s) {
-    if (cplx) return fftl ? launch_tiles<NP, true, true>(ta, s) : launch_tiles<NP, true, false>(ta, s);
-    return fftl ? launch_tiles<NP, false, true>(ta, s) : launch_tiles<NP, false, false>(ta, s);
+int dispatch_tiles(const TileArgs &ta, int64_t n_bound, bool cplx, bool fftl, cudaStream_t s) {
+    if (cplx) return fftl ? launch_tiles<NP, true, true>(ta, n_bound, s) : launch_tiles<NP, true, false>(ta, n_bound, s);
+    return fftl ? launch_tiles<NP, false, true>(ta, n_bound, s) : launch_tiles<NP, false, false>(ta, n_bound, s);
 }
 
 __global__ void k_cell_indices(int64_t n_rows, int64_t C, const double *uvw, const double *freq, int64_t nu, int64_t nv,
@@ -749,6 +931,7 @@ extern "C" int ngg_grid_ps(const NggGridArgs *a, void *stream) {
     float4 *uvs = nullptr, *bbox = nullptr;
     if (C > 0 && (rc = sc.get((void **)&chan, sizeof(ChanParms) * C)) != NGG_OK) return rc;
     const int64_t n_chunks = C * B * nk;
+    if (n_chunks >= (int64_t)1 << 32) return fail(NGG_ERR_UNSUPPORTED, "more than 2^32 track chunks");
     int64_t n_keys = 0;
     unsigned long long *keys_sorted = nullptr;
     const int64_t n_bins = (int64_t)n_img * ntu * ntv;
@@ -801,8 +984,36 @@ extern "C" int ngg_grid_ps(const NggGridArgs *a, void *stream) {
     NGG_CHECK_LAUNCH("k_bounds");
 
     int *counter = nullptr;
-    if ((rc = sc.get((void **)&counter, sizeof(int) * 64)) != NGG_OK) return rc;
-    NGG_CUDA(cudaMemsetAsync(counter, 0, sizeof(int) * 64, s));
+    if ((rc = sc.get((void **)&counter, sizeof(int) * 128)) != NGG_OK) return rc;
+    NGG_CUDA(cudaMemsetAsync(counter, 0, sizeof(int) * 128, s));
+    int *bbox_d = nullptr;
+    if ((rc = sc.get((void **)&bbox_d, sizeof(int) * 4)) != NGG_OK) return rc;
+    k_bbox_init<<<1, 1, 0, s>>>(bbox_d);
+    k_bbox<<<(unsigned)((n_bins + 255) / 256), 256, 0, s>>>(bin_start, n_bins, (int64_t)ntu * ntv, ntv, bbox_d);
+    NGG_CHECK_LAUNCH("k_bbox");
+    // tile work items: every (tile in the busy box, channel); bins with more
+    // than MAXE entries become several items
+    const int64_t n_bound = n_bins;   // box items <= bins
+    int *nsub = nullptr, *soff = nullptr, *n_subs_d = nullptr;
+    SubItem *subs = nullptr;
+    if ((rc = sc.get((void **)&nsub, sizeof(int) * (n_bound + 1))) != NGG_OK) return rc;
+    if ((rc = sc.get((void **)&soff, sizeof(int) * (n_bound + 1))) != NGG_OK) return rc;
+    if ((rc = sc.get((void **)&n_subs_d, sizeof(int))) != NGG_OK) return rc;
+    const int64_t max_subs = n_bound + n_keys / MAXE + 2;
+    if (max_subs >= ((int64_t)1 << 31)) return fail(NGG_ERR_UNSUPPORTED, "too many tile work items");
+    if ((rc = sc.get((void **)&subs, sizeof(SubItem) * max_subs)) != NGG_OK) return rc;
+    k_nsub<<<(unsigned)((n_bound + 1 + 255) / 256), 256, 0, s>>>(bin_start, bbox_d, n_img, (int64_t)ntu * ntv, ntv,
+                                                                n_bound, nsub);
+    NGG_CHECK_LAUNCH("k_nsub");
+    {
+        size_t tb = 0;
+        NGG_CUDA(cub::DeviceScan::ExclusiveSum(nullptr, tb, nsub, soff, n_bound + 1, s));
+        void *tmp2 = nullptr;
+        if ((rc = sc.get(&tmp2, tb)) != NGG_OK) return rc;
+        NGG_CUDA(cub::DeviceScan::ExclusiveSum(tmp2, tb, nsub, soff, n_bound + 1, s));
+    }
+    k_fill_subs<<<(unsigned)((n_bound + 1 + 255) / 256), 256, 0, s>>>(nsub, soff, n_bound + 1, subs, n_subs_d);
+    NGG_CHECK_LAUNCH("k_fill_subs");
     prof_record(1, s);
 
     TileArgs ta;
@@ -823,12 +1034,16 @@ extern "C" int ngg_grid_ps(const NggGridArgs *a, void *stream) {
     ta.tab_len = tab_len;
     ta.tab_bytes = tab_bytes;
     ta.continuum = a->chan_mode == NGG_CHAN_CONTINUUM;
+    ta.bbox = bbox_d;
+    ta.subs = subs;
+    ta.n_subs = n_subs_d;
+    ta.bnk = (unsigned)(B * nk);
     (void)elem;
     for (int64_t p0 = 0, launch = 0; p0 < P; ++launch) {
         const int np = (P - p0) >= 2 ? 2 : 1;
         ta.p0 = (int)p0;
-        ta.work_counter = counter + launch;
-        rc = np == 2 ? dispatch_tiles<2>(ta, cplx, fftl, s) : dispatch_tiles<1>(ta, cplx, fftl, s);
+        ta.work_counter = counter + 2 * launch;
+        rc = np == 2 ? dispatch_tiles<2>(ta, n_bound, cplx, fftl, s) : dispatch_tiles<1>(ta, n_bound, cplx, fftl, s);
         if (rc != NGG_OK) return rc;
         p0 += np;
         if (launch >= 63) return fail(NGG_ERR_UNSUPPORTED, "too many polarizations");

@@ -56,6 +56,7 @@ SIGNATURES = {
     'ngg_fft_correct_adjoint': (ctypes.c_int, [_vp, ctypes.c_int, _i64, _i64, _i64, _i64, _i64, _i64,
                                                _vp, _vp, _vp, _vp]),
     'ngg_degrid_ps': (ctypes.c_int, [ctypes.POINTER(NggDegridArgs), _vp]),
+    'ngg_degrid_ps_noalloc': (ctypes.c_int, [ctypes.POINTER(NggDegridArgs), _vp]),
     'ngg_cell_indices': (ctypes.c_int, [_i64, _i64, _vp, _vp, _i64, _i64, ctypes.POINTER(ctypes.c_double),
                                         ctypes.c_int, ctypes.c_int, _vp, _vp, _vp]),
     'ngg_set_profiling': (None, [ctypes.c_int]),

@@ -10,6 +10,9 @@
 // One thread per (time, baseline, channel) row, channels fastest so weight
 // and visibility accesses are coalesced; the 7 rows of a footprint are 7
 // contiguous 56-byte runs of the grid.
+#include <mutex>
+#include <string>
+
 #include "ngg_internal.cuh"
 
 namespace ngg {
@@ -152,5 +155,97 @@ extern "C" int ngg_degrid_ps(const NggDegridArgs *a, void *stream) {
     scratch_free(uvs, s);
     scratch_free(chan, s);
     if (e != cudaSuccess) return cuda_fail(e, "k_degrid");
+    return NGG_OK;
+}
+
+// ---------------------------------------------------------------------------
+// Degridding without any device allocation.
+//
+// Some programs embed this library inside a host application that owns all
+// device memory: the application sizes its pools up front and forbids
+// allocations it did not make (they could exceed the budget it enforces or
+// fail mid-run, where it cannot recover). ngg_degrid_ps allocates two small
+// scratch arrays per call; this variant keeps them instead in one fixed
+// device array that is part of the library image. The array exists on every
+// GPU that loads the library, for the life of the process.
+//
+// Limits: n_time*n_baseline <= NGG_NOALLOC_MAX_ROWS uvw rows and
+// n_chan <= NGG_NOALLOC_MAX_CHAN channels (16.5 MiB in total).
+// All calls share the array. Every byte a call reads from it is written by
+// that same call first, so nothing has to start at zero, but two calls whose
+// work overlaps on the GPU (different streams, or devices sharing a context)
+// overwrite each other's scratch and give wrong results.
+// ---------------------------------------------------------------------------
+namespace ngg {
+namespace {
+constexpr int64_t kNoAllocRows = NGG_NOALLOC_MAX_ROWS;
+constexpr int64_t kNoAllocChan = NGG_NOALLOC_MAX_CHAN;
+constexpr size_t kNoAllocBytes = sizeof(float4) * kNoAllocRows + sizeof(DChan) * kNoAllocChan;
+
+static __device__ __align__(256) unsigned char g_noalloc_scratch[kNoAllocBytes];
+
+std::mutex g_noalloc_mu;
+void *g_noalloc_ptr[64] = {nullptr};
+
+// Device address of g_noalloc_scratch on the current device (looked up once
+// per device; the host-side symbol itself is not a device address).
+int noalloc_scratch(void **out) {
+    int dev = 0;
+    NGG_CUDA(cudaGetDevice(&dev));
+    if (dev < 0 || dev >= 64) return fail(NGG_ERR_UNSUPPORTED, "device index >= 64");
+    std::lock_guard<std::mutex> lk(g_noalloc_mu);
+    if (!g_noalloc_ptr[dev]) {
+        void *p = nullptr;
+        cudaError_t e = cudaGetSymbolAddress(&p, g_noalloc_scratch);
+        if (e != cudaSuccess) return cuda_fail(e, "cudaGetSymbolAddress(g_noalloc_scratch)");
+        g_noalloc_ptr[dev] = p;
+    }
+    *out = g_noalloc_ptr[dev];
+    return NGG_OK;
+}
+}  // namespace
+}  // namespace ngg
+
+extern "C" int ngg_degrid_ps_noalloc(const NggDegridArgs *a, void *stream) {
+    clear_error();
+    if (!a) return fail(NGG_ERR_INVALID, "args is NULL");
+    cudaStream_t s = (cudaStream_t)stream;
+    if (a->chan_mode != NGG_CHAN_CUBE && a->chan_mode != NGG_CHAN_CONTINUUM) return fail(NGG_ERR_INVALID, "chan_mode");
+    if (a->layout != NGG_LAYOUT_NATURAL && a->layout != NGG_LAYOUT_FFT) return fail(NGG_ERR_INVALID, "layout");
+    if (a->support != SUP) return fail(NGG_ERR_UNSUPPORTED, "support must be 7");
+    if (a->oversampling < 1 || a->oversampling > 1000) return fail(NGG_ERR_UNSUPPORTED, "oversampling out of [1,1000]");
+    const int64_t T = a->n_time, B = a->n_baseline, C = a->n_chan, P = a->n_pol;
+    if (T < 0 || B < 0 || C < 0 || P < 1 || a->n_u < 1 || a->n_v < 1 || a->n_u > 65535 || a->n_v > 65535)
+        return fail(NGG_ERR_INVALID, "dims");
+    if (T * B > kNoAllocRows)
+        return fail(NGG_ERR_INVALID, "ngg_degrid_ps_noalloc: n_time*n_baseline = " + std::to_string(T * B) +
+                                         " exceeds the fixed scratch limit of " + std::to_string(kNoAllocRows) +
+                                         " uvw rows (use ngg_degrid_ps)");
+    if (C > kNoAllocChan)
+        return fail(NGG_ERR_INVALID, "ngg_degrid_ps_noalloc: n_chan = " + std::to_string(C) +
+                                         " exceeds the fixed scratch limit of " + std::to_string(kNoAllocChan) +
+                                         " channels (use ngg_degrid_ps)");
+    if (T * B * C == 0) return NGG_OK;
+    if (!a->grid || !a->uvw || !a->freq || !a->cgk_1D || !a->vis) return fail(NGG_ERR_INVALID, "NULL pointer");
+    const int tab_len = a->oversampling * (a->support / 2 + 1);
+    if (tab_len > 4096) return fail(NGG_ERR_UNSUPPORTED, "kernel table too long");
+    void *base = nullptr;
+    int rc = noalloc_scratch(&base);
+    if (rc != NGG_OK) return rc;
+    float4 *uvs = reinterpret_cast<float4 *>(base);
+    DChan *chan = reinterpret_cast<DChan *>(reinterpret_cast<unsigned char *>(base) + sizeof(float4) * kNoAllocRows);
+    k_dchan<<<(unsigned)((C + 127) / 128), 128, 0, s>>>(a->freq, (int)C, a->delta_lm[0], a->delta_lm[1], a->n_u, a->n_v, chan);
+    k_dsplit<<<(unsigned)((T * B + 255) / 256), 256, 0, s>>>(a->uvw, T, B, uvs);
+    const int64_t n = T * B * C;
+    const int cont = a->chan_mode == NGG_CHAN_CONTINUUM;
+    if (a->layout == NGG_LAYOUT_FFT)
+        k_degrid<true><<<(unsigned)((n + 255) / 256), 256, 0, s>>>((const float2 *)a->grid, a->uvw, uvs, a->weight, chan,
+                                                                    a->cgk_1D, tab_len, a->oversampling, T, B, C, P,
+                                                                    a->n_u, a->n_v, cont, (float2 *)a->vis);
+    else
+        k_degrid<false><<<(unsigned)((n + 255) / 256), 256, 0, s>>>((const float2 *)a->grid, a->uvw, uvs, a->weight, chan,
+                                                                     a->cgk_1D, tab_len, a->oversampling, T, B, C, P,
+                                                                     a->n_u, a->n_v, cont, (float2 *)a->vis);
+    NGG_CHECK_LAUNCH("k_degrid (noalloc)");
     return NGG_OK;
 }

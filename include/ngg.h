@@ -192,6 +192,20 @@ typedef struct NggDegridArgs {
 
 int ngg_degrid_ps(const NggDegridArgs *args, void *stream);
 
+/* ngg_degrid_ps_noalloc: the same result as ngg_degrid_ps, for callers that
+ * must not have the library allocate device memory (e.g. a host application
+ * that owns and budgets all device memory itself). No counterpart in the
+ * reference. Its scratch is a fixed array inside the library (present on
+ * every GPU that loads libngg.so until the process exits), so sizes are
+ * limited: n_time*n_baseline <= NGG_NOALLOC_MAX_ROWS and
+ * n_chan <= NGG_NOALLOC_MAX_CHAN, else NGG_ERR_INVALID. The first call on a
+ * device looks up that array's device address (cudaGetSymbolAddress); make
+ * that first call before any stream capture. Calls share the array: calls
+ * whose GPU work overlaps (e.g. on two streams) corrupt each other. */
+#define NGG_NOALLOC_MAX_ROWS 1048576
+#define NGG_NOALLOC_MAX_CHAN 16384
+int ngg_degrid_ps_noalloc(const NggDegridArgs *args, void *stream);
+
 int ngg_fft_correct_adjoint(const void *image, int image_is_f64, int64_t n_chan_img, int64_t n_pol,
                             int64_t n_u, int64_t n_v, int64_t n_l, int64_t n_m,
                             const double *sum_weight, const double *correction, void *grid,

@@ -41,6 +41,17 @@ class NggDegridArgs(ctypes.Structure):
                 ('grid', _vp), ('uvw', _vp), ('weight', _vp), ('freq', _vp), ('cgk_1D', _vp), ('vis', _vp)]
 
 
+class NggGcfArgs(ctypes.Structure):
+    _fields_ = [('mode', ctypes.c_int), ('chan_mode', ctypes.c_int), ('layout', ctypes.c_int),
+                ('oversampling', ctypes.c_int * 2), ('n_field', ctypes.c_int),
+                ('n_time', _i64), ('n_baseline', _i64), ('n_chan', _i64), ('n_pol', _i64),
+                ('n_u', _i64), ('n_v', _i64), ('delta_lm', ctypes.c_double * 2),
+                ('n_cf_baseline', _i64), ('n_cf_chan', _i64), ('n_cf_pol', _i64), ('conv_size', _i64 * 2),
+                ('vis', _vp), ('uvw', _vp), ('weight', _vp), ('freq', _vp), ('field_index', _vp),
+                ('cf_baseline_map', _vp), ('cf_chan_map', _vp), ('cf_pol_map', _vp),
+                ('conv_kernel', _vp), ('support', _vp), ('phase_slope', _vp), ('grid', _vp), ('sum_weight', _vp)]
+
+
 # exported symbol -> (restype, argtypes)
 SIGNATURES = {
     'ngg_version': (ctypes.c_int, []),
@@ -59,6 +70,14 @@ SIGNATURES = {
     'ngg_degrid_ps_noalloc': (ctypes.c_int, [ctypes.POINTER(NggDegridArgs), _vp]),
     'ngg_cell_indices': (ctypes.c_int, [_i64, _i64, _vp, _vp, _i64, _i64, ctypes.POINTER(ctypes.c_double),
                                         ctypes.c_int, ctypes.c_int, _vp, _vp, _vp]),
+    'ngg_grid_gcf': (ctypes.c_int, [ctypes.POINTER(NggGcfArgs), _vp]),
+    'ngg_grid_gcf_weight': (ctypes.c_int, [ctypes.POINTER(NggGcfArgs), _vp]),
+    'ngg_gcf_kernels': (ctypes.c_int, [ctypes.c_int, _i64, _vp, _vp, _i64, _vp, _i64, _vp, _i64, _i64,
+                                       ctypes.POINTER(ctypes.c_double), _i64, _i64, _vp, _vp, _vp]),
+    'ngg_mosaic_normalize': (ctypes.c_int, [_vp, _i64, _i64, _i64, _vp, _vp, _vp, ctypes.c_double,
+                                            ctypes.POINTER(ctypes.c_int), ctypes.c_int,
+                                            ctypes.POINTER(ctypes.c_int64), _vp]),
+    'ngg_sqrt_abs': (ctypes.c_int, [_vp, _i64, _vp, _vp]),
     'ngg_set_profiling': (None, [ctypes.c_int]),
     'ngg_last_phase_ms': (ctypes.c_int, [ctypes.POINTER(ctypes.c_double), ctypes.POINTER(ctypes.c_double)]),
     'ngg_release_cache': (None, []),
@@ -283,6 +302,136 @@ def cell_indices(uvw_rows, freq, n_uv, delta_lm, oversampling, mirror=False):
                                    int(oversampling), 1 if mirror else 0, _ptr(idx), _ptr(nfb), _stream()),
            'ngg_cell_indices')
     return idx, int(nfb.item())
+
+
+def _gcf_args(uvw_t, w_t, f_t, fidx_t, maps, ck_t, sup_t, slope_t, n_uv, delta_lm, oversampling, chan_mode,
+              layout, mode):
+    T, B, C, P = w_t.shape
+    a = NggGcfArgs()
+    a.mode = MODES[mode]
+    a.chan_mode = CHAN_MODES[chan_mode]
+    a.layout = LAYOUTS[layout]
+    a.oversampling[0], a.oversampling[1] = int(oversampling[0]), int(oversampling[1])
+    a.n_field = int(slope_t.shape[0])
+    a.n_time, a.n_baseline, a.n_chan, a.n_pol = T, B, C, P
+    a.n_u, a.n_v = int(n_uv[0]), int(n_uv[1])
+    a.delta_lm[0], a.delta_lm[1] = float(delta_lm[0]), float(delta_lm[1])
+    a.n_cf_baseline, a.n_cf_chan, a.n_cf_pol = (int(x) for x in ck_t.shape[:3])
+    a.conv_size[0], a.conv_size[1] = int(ck_t.shape[3]), int(ck_t.shape[4])
+    a.uvw = _ptr(uvw_t).value
+    a.weight = _ptr(w_t).value
+    a.freq = _ptr(f_t).value
+    a.field_index = _ptr(fidx_t).value
+    a.cf_baseline_map, a.cf_chan_map, a.cf_pol_map = (_ptr(m).value for m in maps)
+    a.conv_kernel = _ptr(ck_t).value
+    a.support = _ptr(sup_t).value
+    a.phase_slope = _ptr(slope_t).value
+    return a
+
+
+def _gcf_inputs(uvw, weight, freq, field_index, cf_baseline_map, cf_chan_map, cf_pol_map, conv_kernel, support,
+                phase_slope):
+    torch = _torch()
+    uvw_t = _dev(uvw, torch.float64, 'uvw')
+    w_t = _dev(weight, torch.float32, 'weight')
+    f_t = _dev(freq, torch.float64, 'freq')
+    fidx_t = _dev(field_index, torch.int32, 'field_index')
+    maps = [_dev(m, torch.int32, n) for m, n in ((cf_baseline_map, 'cf_baseline_map'), (cf_chan_map, 'cf_chan_map'),
+                                                 (cf_pol_map, 'cf_pol_map'))]
+    ck_t = _dev(conv_kernel, torch.float64, 'conv_kernel')
+    sup_t = _dev(support, torch.int32, 'support')
+    slope_t = _dev(phase_slope, torch.float64, 'phase_slope')
+    if ck_t.dim() != 5 or tuple(sup_t.shape) != tuple(ck_t.shape[:3]) + (2,):
+        raise NggError('conv_kernel must be (n_cf_baseline, n_cf_chan, n_cf_pol, R0, R1) and support (..., 2)')
+    T, B, C, P = w_t.shape
+    if tuple(fidx_t.shape) != (T, B) or maps[0].numel() != B or maps[1].numel() != C or maps[2].numel() != P:
+        raise NggError('field_index must be (T, B) and the CF maps (B,), (C,), (P,)')
+    return uvw_t, w_t, f_t, fidx_t, maps, ck_t, sup_t, slope_t
+
+
+def grid_gcf(vis, uvw, weight, freq, field_index, cf_baseline_map, cf_chan_map, cf_pol_map, conv_kernel, support,
+             phase_slope, n_uv, delta_lm, oversampling, mode='data', chan_mode='cube', layout='natural'):
+    """Mosaic gridder with a GCF table: (grid complex64 (Cimg,P,Nu,Nv), sum_weight (Cimg,P) f64)."""
+    torch = _torch()
+    ins = _gcf_inputs(uvw, weight, freq, field_index, cf_baseline_map, cf_chan_map, cf_pol_map, conv_kernel,
+                      support, phase_slope)
+    w_t = ins[1]
+    T, B, C, P = w_t.shape
+    v_t = _dev(vis, torch.complex64, 'vis') if mode == 'data' else None
+    n_img = 1 if chan_mode == 'continuum' else C
+    grid = torch.empty((n_img, P, int(n_uv[0]), int(n_uv[1])), dtype=torch.complex64, device='cuda')
+    sw = torch.empty((n_img, P), dtype=torch.float64, device='cuda')
+    a = _gcf_args(*ins, n_uv, delta_lm, oversampling, chan_mode, layout, mode)
+    a.vis = _ptr(v_t).value
+    a.grid = _ptr(grid).value
+    a.sum_weight = _ptr(sw).value
+    _check(load().ngg_grid_gcf(ctypes.byref(a), _stream()), 'ngg_grid_gcf')
+    return grid, sw
+
+
+def grid_gcf_weight(uvw, weight, freq, field_index, cf_baseline_map, cf_chan_map, cf_pol_map, weight_conv_kernel,
+                    support, phase_slope, n_uv, delta_lm, oversampling, chan_mode='cube', layout='natural'):
+    """Mosaic weight grid (every tap at the grid centre): (grid, sum_weight)."""
+    torch = _torch()
+    ins = _gcf_inputs(uvw, weight, freq, field_index, cf_baseline_map, cf_chan_map, cf_pol_map, weight_conv_kernel,
+                      support, phase_slope)
+    T, B, C, P = ins[1].shape
+    n_img = 1 if chan_mode == 'continuum' else C
+    grid = torch.empty((n_img, P, int(n_uv[0]), int(n_uv[1])), dtype=torch.complex64, device='cuda')
+    sw = torch.empty((n_img, P), dtype=torch.float64, device='cuda')
+    a = _gcf_args(*ins, n_uv, delta_lm, oversampling, chan_mode, layout, 'psf')
+    a.grid = _ptr(grid).value
+    a.sum_weight = _ptr(sw).value
+    _check(load().ngg_grid_gcf_weight(ctypes.byref(a), _stream()), 'ngg_grid_gcf_weight')
+    return grid, sw
+
+
+def gcf_kernels(function, dish_diameters, blockage_diameters, pairs, freq, n, cell, center):
+    """FP64 baseline GCFs before cropping: (conv_kernel, weight_conv_kernel), each (n_pairs, n_freq, n0, n1)."""
+    torch = _torch()
+    d_t = _dev(np.asarray(dish_diameters, dtype=np.float64), torch.float64, 'dish_diameters')
+    b_t = _dev(np.asarray(blockage_diameters, dtype=np.float64), torch.float64, 'blockage_diameters')
+    p_t = _dev(np.asarray(pairs, dtype=np.int32).reshape(-1, 2), torch.int32, 'pairs')
+    f_t = _dev(np.asarray(freq, dtype=np.float64), torch.float64, 'freq')
+    n0, n1 = int(n[0]), int(n[1])
+    npair, nf = int(p_t.shape[0]), int(f_t.shape[0])
+    ck = torch.empty((npair, nf, n0, n1), dtype=torch.float64, device='cuda')
+    wk = torch.empty_like(ck)
+    _check(load().ngg_gcf_kernels(1 if function == 'casa_airy' else 0, int(d_t.shape[0]), _ptr(d_t), _ptr(b_t),
+                                  npair, _ptr(p_t), nf, _ptr(f_t), n0, n1, _dl(cell), int(center[0]), int(center[1]),
+                                  _ptr(ck), _ptr(wk), _stream()), 'ngg_gcf_kernels')
+    return ck, wk
+
+
+def mosaic_normalize(image, ps_corr=None, norm_image=None, pb=None, pb_limit=0.0, oversampling=(1, 1),
+                     single_precision=False, centre=None):
+    """In-place mosaic normalisation of image (l, m, C, P) float64 (see ngg.h)."""
+    torch = _torch()
+    if image.dtype != torch.float64 or not image.is_cuda or not image.is_contiguous():
+        raise NggError('image must be a contiguous float64 CUDA tensor')
+    nl, nm = int(image.shape[0]), int(image.shape[1])
+    npl = int(image.numel() // max(nl * nm, 1))
+    ps_t = _dev(ps_corr, torch.float64, 'ps_corr', allow_none=True)
+    n_t = _dev(norm_image, torch.float64, 'norm_image', allow_none=True)
+    pb_t = _dev(pb, torch.float64, 'pb', allow_none=True)
+    for t, n in ((n_t, 'norm_image'), (pb_t, 'pb')):
+        if t is not None and t.numel() != image.numel():
+            raise NggError(f'{n} must have the shape of image')
+    if ps_t is not None and ps_t.numel() != nl * nm:
+        raise NggError('ps_corr must be (n_l, n_m)')
+    os_ = (ctypes.c_int * 2)(int(oversampling[0]), int(oversampling[1]))
+    cen = (ctypes.c_int64 * 2)(int(centre[0]), int(centre[1])) if centre is not None else None
+    _check(load().ngg_mosaic_normalize(_ptr(image), nl, nm, npl, _ptr(ps_t), _ptr(n_t), _ptr(pb_t), float(pb_limit),
+                                       os_, 1 if single_precision else 0, cen, _stream()), 'ngg_mosaic_normalize')
+    return image
+
+
+def sqrt_abs(x):
+    torch = _torch()
+    x = _dev(x, torch.float64, 'x')
+    out = torch.empty_like(x)
+    _check(load().ngg_sqrt_abs(_ptr(x), int(x.numel()), _ptr(out), _stream()), 'ngg_sqrt_abs')
+    return out
 
 
 def set_profiling(enable=True):

@@ -80,3 +80,23 @@ def _check_norm_parms(p):
     ok &= _check(p, 'single_precision', bool, default=True)
     ok &= _check(p, 'pb_limit', numbers.Number, default=0.2)
     return bool(ok)
+
+
+def _check_gcf_parms(p):
+    """_check_imaging_parms.py:45-84: defaults and array conversion of gcf_parms."""
+    ok = _check(p, 'function', str, default='casa_airy', acceptable=['casa_airy', 'airy'])
+    for k in ('freq_chan', 'list_dish_diameters', 'list_blockage_diameters', 'unique_ant_indx', 'pol'):
+        ok &= _check(p, k, None, list_len=-1, elem_types=numbers.Number)
+    ok &= _check(p, 'chan_tolerance_factor', numbers.Number, default=0.005)
+    ok &= _check(p, 'oversampling', None, default=[10, 10], list_len=2, elem_types=_INT)
+    ok &= _check(p, 'max_support', None, default=[15, 15], list_len=2, elem_types=_INT)
+    ok &= _check(p, 'support_cut_level', numbers.Number, default=2.5e-2)
+    ok &= _check(p, 'a_chan_num_chunk', _INT, default=3)
+    if ok and len(p['list_dish_diameters']) != len(p['list_blockage_diameters']):
+        ok = _err('Parameter list_dish_diameters and list_blockage_diameters must be the same length.')
+    if ok:
+        p['oversampling'] = np.array(p['oversampling']).astype(int)
+        p['max_support'] = np.array(p['max_support']).astype(int)
+        for k in ('freq_chan', 'list_dish_diameters', 'list_blockage_diameters', 'unique_ant_indx', 'pol'):
+            p[k] = np.array(p[k])
+    return bool(ok)

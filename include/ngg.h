@@ -211,6 +211,89 @@ int ngg_fft_correct_adjoint(const void *image, int image_is_f64, int64_t n_chan_
                             const double *sum_weight, const double *correction, void *grid,
                             void *stream);
 
+/* ---- mosaic (aperture-projection) gridding with a GCF table ---------------
+ * Replaces _aperture_grid_numpy_wrap / _aperture_psf_grid_numpy_wrap /
+ * _aperture_grid_jit (ngcasa/imaging/_imaging_utils/_aperture_grid.py:294-513)
+ * and _aperture_weight_grid_jit (:146-291).
+ *
+ * conv_kernel: float64 (n_cf_baseline, n_cf_chan, n_cf_pol, R0, R1), the
+ * CONV_KERNEL (or WEIGHT_CONV_KERNEL) table of make_gridding_convolution_function;
+ * support: int32 (n_cf_baseline, n_cf_chan, n_cf_pol, 2). The phase gradient
+ * of field f is exp(i*(x*phase_slope[f,0] + y*phase_slope[f,1])) with (x, y)
+ * the table offsets from its centre (R0/2, R1/2) -- the table
+ * make_phase_gradient builds (make_gridding_convolution_function.py:331-359).
+ * field_index: int32 (T, B), the index into the field list of each row's
+ * FIELD_ID, or -1 to skip the row. Maps: cf_baseline_map int32 (B),
+ * cf_chan_map int32 (C), cf_pol_map int32 (P). weight = imaging weights.
+ * Taps: table[cfb,cfc,cfp, os0*iu + off_u + R0/2, os1*iv + off_v + R1/2] times
+ * the phase gradient, |iu|,|iv| <= support/2; a row is skipped when any cell
+ * within max(support) of its centre leaves the grid (the reference's rule).
+ * sum_weight: weight*Re(norm^2) (DATA) or weight*Re(norm) (PSF), norm = sum
+ * of the row's complex taps. Grid complex64 (Cimg, P, Nu, Nv), overwritten.
+ * ngg_grid_gcf_weight: the weight grid of make_mosaic_pb: every tap placed
+ * at the grid centre, sum_weight += weight*Re(norm). */
+typedef struct NggGcfArgs {
+    int mode;          /* NGG_MODE_DATA | NGG_MODE_PSF (ignored by the weight grid) */
+    int chan_mode;
+    int layout;
+    int oversampling[2];
+    int n_field;
+    int64_t n_time, n_baseline, n_chan, n_pol;
+    int64_t n_u, n_v;
+    double delta_lm[2];
+    int64_t n_cf_baseline, n_cf_chan, n_cf_pol;
+    int64_t conv_size[2];        /* R0, R1 */
+    const void *vis;             /* complex64 (T,B,C,P); NULL for PSF / weight */
+    const double *uvw;           /* float64 (T,B,3)            */
+    const float *weight;         /* float32 (T,B,C,P)          */
+    const double *freq;          /* float64 (C)                */
+    const int32_t *field_index;  /* int32 (T,B)                */
+    const int32_t *cf_baseline_map, *cf_chan_map, *cf_pol_map;
+    const double *conv_kernel;   /* float64 (ncfb,ncfc,ncfp,R0,R1) */
+    const int32_t *support;      /* int32 (ncfb,ncfc,ncfp,2)   */
+    const double *phase_slope;   /* float64 (n_field, 2)       */
+    void *grid;                  /* complex64 (Cimg,P,Nu,Nv)   */
+    double *sum_weight;          /* float64 (Cimg,P)           */
+} NggGcfArgs;
+
+int ngg_grid_gcf(const NggGcfArgs *args, void *stream);
+int ngg_grid_gcf_weight(const NggGcfArgs *args, void *stream);
+
+/* GCF generation helpers (make_gridding_convolution_function.py:181-246 with
+ * _make_pb_symmetric.py:79-235): for every antenna pair and PB frequency,
+ * the pair's voltage pattern product on an n0 x n1 grid of `cell` (radians,
+ * the image cell times the GCF oversampling) centred at (c0, c1) -- Airy
+ * disk of dish and blockage diameters, CASA form (casa_model = 1) or the
+ * textbook obscured form (0) -- and the real part of its centred FFT,
+ * real(fftshift(fft2(ifftshift(pattern^ipower)))) for ipower 1 (conv_kernel)
+ * and 2 (weight_conv_kernel), in FP64. pairs: int32 (n_pairs, 2) indices
+ * into the diameter lists. Outputs float64 (n_pairs, n_freq, n0, n1). */
+int ngg_gcf_kernels(int casa_model, int64_t n_types, const double *dish_diameters,
+                    const double *blockage_diameters, int64_t n_pairs, const int32_t *pairs,
+                    int64_t n_freq, const double *freq, int64_t n0, int64_t n1,
+                    const double cell[2], int64_t c0, int64_t c1, double *conv_kernel,
+                    double *weight_conv_kernel, void *stream);
+
+/* Mosaic normalisation (make_image_with_gcf / make_psf_with_gcf through
+ * _normalize, ngcasa/imaging/_imaging_utils/_normalize.py:14-90, forward
+ * direction), in place on image float64 (n_l, n_m, n_planes) that already
+ * holds Re(FFT^-1 grid) * Nu*Nv / sum_weight (ngg_fft_correct with a
+ * correction of ones): image / (osc * (ps_corr * norm_image)) with
+ * osc(l, m) = sinc((l - n_l/2) / (n_l os0)) * sinc((m - n_m/2) / (n_m os1)),
+ * ps_corr (n_l, n_m) or NULL (ones), norm_image (n_l, n_m, n_planes) or NULL
+ * (ones: norm_type 'none'; PB for 'flat_noise', WEIGHT_PB for 'flat_sky');
+ * then 0 where pb < pb_limit (pb_limit > 0 and pb not NULL), then rounded
+ * through float32 if single_precision. If centre is not NULL every plane is
+ * finally divided by its value at (centre[0], centre[1]) (the PSF,
+ * make_psf_with_gcf.py:99). */
+int ngg_mosaic_normalize(double *image, int64_t n_l, int64_t n_m, int64_t n_planes,
+                         const double *ps_corr, const double *norm_image, const double *pb,
+                         double pb_limit, const int oversampling[2], int single_precision,
+                         const int64_t *centre, void *stream);
+
+/* out[i] = sqrt(|x[i]|): the mosaic PB from WEIGHT_PB (make_mosaic_pb.py:150). */
+int ngg_sqrt_abs(const double *x, int64_t n, double *out, void *stream);
+
 /* Profiling: when enabled, ngg_grid_ps records CUDA events on its stream
  * around its binning phase and its tile-accumulation kernels. ngg_last_phase_ms
  * waits for the last call's events and returns the two durations (ms). */

@@ -131,5 +131,93 @@ def main():
         print(k, v)
 
 
+def sin_pixel_offsets(field_phase_dir, phase_center, npad, cell_rad):
+    """Pixel offsets of field centres in the SIN projection of the padded grid
+    (the reference evaluates this with astropy's all_world2pix,
+    make_gridding_convolution_function.py:331-347; restated here)."""
+    a0, d0 = phase_center
+    a, d = field_phase_dir[:, 0], field_phase_dir[:, 1]
+    l = np.cos(d) * np.sin(a - a0)
+    m = np.sin(d) * np.cos(d0) - np.cos(d) * np.sin(d0) * np.cos(a - a0)
+    rad_to_deg = 180 / np.pi
+    cdelt = np.asarray(cell_rad) * rad_to_deg
+    return np.stack([np.rad2deg(l) / cdelt[0], np.rad2deg(m) / cdelt[1]], axis=1)
+
+
+def phase_gradient(field_phase_dir, phase_center, npad, cell_rad, oversampling, resize_conv_size):
+    pix_dist = sin_pixel_offsets(field_phase_dir, phase_center, npad, cell_rad)
+    pix = -pix_dist * 2 * np.pi / (np.asarray(npad) * np.asarray(oversampling))
+    c = np.asarray(resize_conv_size) // 2
+    x = np.arange(-c[0], resize_conv_size[0] - c[0])
+    y = np.arange(-c[1], resize_conv_size[1] - c[1])
+    xg, yg = np.meshgrid(x, y, indexing='ij')
+    return np.moveaxis(np.exp(1j * (xg[:, :, None] * pix[:, 0] + yg[:, :, None] * pix[:, 1])), 2, 0)
+
+
+def mosaic_case(R):
+    rng = np.random.default_rng(31)
+    n_ant = 6
+    enu = simulate.disk_layout(n_ant, 40.0, rng)
+    T_per = 10
+    n_field = 2
+    T = T_per * n_field
+    uvw = simulate.earth_rotation_uvw(enu, T, 60.0)
+    a1, a2 = simulate.baseline_pairs(n_ant)
+    B = uvw.shape[1]
+    freq = np.array([100.0e9, 100.6e9, 101.2e9])
+    C, P = len(freq), 2
+    vis = (rng.standard_normal((T, B, C, P)) + 1j * rng.standard_normal((T, B, C, P))).astype(np.complex64)
+    iw = rng.uniform(0.5, 2.0, (T, B, C, P))
+    field = np.repeat(np.arange(n_field), T_per)[:, None].repeat(B, axis=1).astype(np.int64)
+    field[3, 4] = -1                        # a row without a field is skipped
+    dec0 = np.deg2rad(-30.0)
+    phase_center = np.array([np.deg2rad(150.0), dec0])
+    off = np.deg2rad(20.0 / 3600)
+    field_phase_dir = np.array([[phase_center[0] - off / np.cos(dec0) / 2, dec0],
+                                [phase_center[0] + off / np.cos(dec0) / 2, dec0]])
+    gp = {'image_size': [64, 64], 'cell_size': [2.0, 2.0], 'chan_mode': 'cube', 'fft_padding': 1.2}
+    assert R.cp._check_grid_parms(gp)
+    gcf = {'function': 'casa_airy', 'list_dish_diameters': [12.0], 'list_blockage_diameters': [0.75],
+           'unique_ant_indx': [0] * n_ant, 'oversampling': [4, 4], 'max_support': [15, 15],
+           'freq_chan': list(freq), 'pol': [0, 1], 'chan_tolerance_factor': 0.005}
+    assert R.cp._check_gcf_parms(gcf)
+    gcf['basline_ant'] = np.stack([a1, a2], axis=1)
+    gcf['resize_conv_size'] = (gcf['max_support'] + 1) * gcf['oversampling']
+    cfb_map, pb_pairs = R.gcf.create_cf_baseline_map(gcf['unique_ant_indx'], gcf['basline_ant'], 1)
+    cfc_map, pb_freq = R.gcf.create_cf_chan_map(freq, gcf['chan_tolerance_factor'])
+    cfp_map = np.zeros(P, dtype=int)
+    gcf['ipower'] = 1
+    bp = R.gcf.make_baseline_patterns(pb_freq, np.array([0]), pb_pairs, R.pb._casa_airy_disk_rorder, gcf, gp)
+    gcf['ipower'] = 2
+    bw = R.gcf.make_baseline_patterns(pb_freq, np.array([0]), pb_pairs, R.pb._casa_airy_disk_rorder, gcf, gp)
+    ck_full = np.real(np.fft.fftshift(np.fft.fft2(np.fft.ifftshift(bp, axes=(3, 4)), axes=(3, 4)), axes=(3, 4)))
+    wk_full = np.real(np.fft.fftshift(np.fft.fft2(np.fft.ifftshift(bw, axes=(3, 4)), axes=(3, 4)), axes=(3, 4)))
+    ck, wk, support = R.gcf.resize_and_calc_support(ck_full, wk_full, gcf, gp)
+    pg = phase_gradient(field_phase_dir, phase_center, gp['image_size_padded'], gp['cell_size'],
+                        gcf['oversampling'], gcf['resize_conv_size'])
+    g = copy.deepcopy(gp)
+    g.update({'oversampling': gcf['oversampling'], 'complex_grid': True, 'do_psf': False,
+              'field_id': np.arange(n_field)})
+    grid, sw = R.ag._aperture_grid_numpy_wrap(vis, uvw, iw, field, cfb_map, cfc_map, cfp_map, ck, support, pg, freq, g)
+    g['do_psf'] = True
+    pgrid, psw = R.ag._aperture_psf_grid_numpy_wrap(uvw, iw, field, cfb_map, cfc_map, cfp_map, ck, support, pg, freq, g)
+    wgrid, wsw = R.ag._aperture_weight_grid_numpy_wrap(uvw, iw, field, cfb_map, cfc_map, cfp_map, wk, support, pg,
+                                                       freq, g)
+    np.savez_compressed(os.path.join(HERE, 'mosaic.npz'), vis=vis, uvw=uvw, imaging_weight=iw, field=field,
+                        freq=freq, antenna1=a1, antenna2=a2, field_phase_dir=field_phase_dir,
+                        phase_center=phase_center, image_size=np.array(gp['image_size']),
+                        cell_arcsec=np.array([2.0, 2.0]), oversampling=gcf['oversampling'],
+                        max_support=gcf['max_support'], cf_baseline_map=cfb_map, cf_chan_map=cfc_map,
+                        cf_pol_map=cfp_map, pb_freq=pb_freq, baseline_pb=bp, weight_baseline_pb=bw,
+                        conv_kernel=ck, weight_conv_kernel=wk, support=support, phase_gradient=pg,
+                        grid=grid, sum_weight=sw, psf_grid=pgrid, psf_sum_weight=psw,
+                        weight_grid=wgrid, weight_sum_weight=wsw)
+    print('mosaic', 'support', support.ravel(), 'pb_freq', pb_freq, 'ck', ck.shape, 'grid', grid.shape,
+          'sw', sw.ravel()[:4])
+
+
 if __name__ == '__main__':
-    main()
+    if len(sys.argv) == 1 or sys.argv[1] == 'standard':
+        main()
+    if len(sys.argv) == 1 or sys.argv[1] == 'mosaic':
+        mosaic_case(refshim.modules())

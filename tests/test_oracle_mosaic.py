@@ -66,6 +66,16 @@ def test_phase_gradient_restatement(gold):
     assert np.isclose(off[1, 1], np.sin(1e-4) / gp['cell_size'][1], rtol=1e-12)
 
 
+def test_sin_projection_known_answer():
+    """The reference's recorded CASA toPixelWCS case
+    (make_gridding_convolution_function.py:569-581): crpix 120, cdelt
+    (-5e-5, 5e-5) deg, crval (180.4684619, -18.8638732472) deg."""
+    pc = np.deg2rad([180.46846189999996568, -18.863873247222226581])
+    world = np.deg2rad([[-179.5337374791666889, -18.863873258333338612]])
+    off = M.sin_pixel_offsets(world, pc, np.deg2rad([-5e-05, 5e-05]))
+    assert np.allclose(120 + off[0], [161.6249842951184803, 119.99951947142589859], rtol=0, atol=1e-9)
+
+
 def test_product_host_logic_matches_oracle(gold):
     import importlib
     G = importlib.import_module('cngi_prototype_gb300.imaging.make_gridding_convolution_function')

@@ -29,18 +29,13 @@
 #include <vector>
 
 #include "ngg_internal.cuh"
+#include "gcf_grid.cuh"
 
 namespace ngg {
 namespace {
 
-constexpr int MAXS = 31;    // largest support (one lane per column class)
-constexpr int SP = 32;      // padded tap run length
-constexpr int GCH = 32;     // time steps per warp item
 
-struct GChan {
-    double su, sv;
-    float suh, sul, svh, svl;
-};
+
 
 __global__ void k_gchan(const double *freq, int C, double dl0, double dl1, int64_t nu, int64_t nv, GChan *out) {
     int c = blockIdx.x * blockDim.x + threadIdx.x;
@@ -60,31 +55,71 @@ __global__ void k_gsplit(const double *uvw, int64_t n, float4 *uvs) {
 
 __device__ __forceinline__ bool in_support(int i, int s) { return i >= -(s / 2) && i < s - s / 2; }
 
-// ckr[cf][ou][ov][iu][iv] (iv padded to SP), zero outside the CF's support
+// ckt[cf][ou][ov][r][col]: tap row r in [0, 2S) holds dv + S/2 = r mod S (each
+// row stored twice, so a rotated run of S rows is contiguous), col = du + S/2
+// in [0, 32) (one per lane); zero outside the CF's support and for col >= S
 __global__ void k_reorg(const double *ck, int64_t ncf, int64_t R0, int64_t R1, int os0, int os1, const int32_t *support,
-                        int S, float *ckr) {
+                        int S, float *ckt) {
     const int64_t id = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
-    const int64_t n = ncf * (os0 + 1) * (os1 + 1) * S * SP;
+    const int64_t n = ncf * (os0 + 1) * (os1 + 1) * 2 * S * SP;
     if (id >= n) return;
     int64_t r = id;
-    const int iv_i = (int)(r % SP); r /= SP;
-    const int iu_i = (int)(r % S); r /= S;
+    const int col = (int)(r % SP); r /= SP;
+    const int row = (int)(r % (2 * S)); r /= 2 * S;
     const int ov_i = (int)(r % (os1 + 1)); r /= (os1 + 1);
     const int ou_i = (int)(r % (os0 + 1)); r /= (os0 + 1);
     const int64_t cf = r;
     const int sc = S / 2;
-    const int iu = iu_i - sc, iv = iv_i - sc;
+    const int iu = col - sc, iv = row % S - sc;
     const int ou = ou_i - os0 / 2, ov = ov_i - os1 / 2;
     float val = 0.f;
-    if (iv_i < S && in_support(iu, support[cf * 2 + 0]) && in_support(iv, support[cf * 2 + 1])) {
+    if (col < S && in_support(iu, support[cf * 2 + 0]) && in_support(iv, support[cf * 2 + 1])) {
         const int64_t x = (int64_t)os0 * iu + ou + R0 / 2, y = (int64_t)os1 * iv + ov + R1 / 2;
         if (x >= 0 && x < R0 && y >= 0 && y < R1) val = (float)ck[(cf * R0 + x) * R1 + y];
     }
-    ckr[id] = val;
+    ckt[id] = val;
 }
 
-// per-field phase tables: ex[f][x] = exp(i (x - R0/2) px_f), ey likewise
-__global__ void k_phase_tabs(const double *slope, int nf, int64_t R0, int64_t R1, float2 *ex, float2 *ey) {
+// Phase gradient factored by grid position: the tap at table offset
+// x' = os0*(u - cu) + ou has phase x' px = os0 u px + ou px - os0 cu px, so a
+// visibility carries Hx[ou] conj(Gx[cu]) (and the same in v) and a grid cell
+// u is rotated by Gx[u] when it is flushed. Gx[f][u] = e^{i os0 u px_f},
+// Hx[f][oi] = e^{i (oi - os0/2) px_f}; arguments in FP64.
+__global__ void k_cell_phase(const double *slope, int nf, int64_t nu, int64_t nv, int os0, int os1, float2 *gx,
+                             float2 *gy, float2 *hx, float2 *hy) {
+    const int64_t per = nu + nv + (os0 + 1) + (os1 + 1);
+    const int64_t id = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (id >= (int64_t)nf * per) return;
+    const int64_t f = id / per;
+    int64_t x = id % per;
+    const double px = slope[f * 2 + 0], py = slope[f * 2 + 1];
+    double s, c;
+    if (x < nu) {
+        sincos((double)os0 * (double)x * px, &s, &c);
+        gx[f * nu + x] = make_float2((float)c, (float)s);
+        return;
+    }
+    x -= nu;
+    if (x < nv) {
+        sincos((double)os1 * (double)x * py, &s, &c);
+        gy[f * nv + x] = make_float2((float)c, (float)s);
+        return;
+    }
+    x -= nv;
+    if (x < os0 + 1) {
+        sincos((double)(x - os0 / 2) * px, &s, &c);
+        hx[f * (os0 + 1) + x] = make_float2((float)c, (float)s);
+        return;
+    }
+    x -= os0 + 1;
+    sincos((double)(x - os1 / 2) * py, &s, &c);
+    hy[f * (os1 + 1) + x] = make_float2((float)c, (float)s);
+}
+
+// per-field phase tables: ex[f][x] = exp(i (x - R0/2) px_f), ey likewise, in
+// FP32 for the taps and FP64 for the tap sums
+__global__ void k_phase_tabs(const double *slope, int nf, int64_t R0, int64_t R1, float2 *ex, float2 *ey,
+                             double2 *ex64, double2 *ey64) {
     const int64_t id = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
     if (id >= (int64_t)nf * (R0 + R1)) return;
     const int64_t f = id / (R0 + R1), x = id % (R0 + R1);
@@ -92,16 +127,19 @@ __global__ void k_phase_tabs(const double *slope, int nf, int64_t R0, int64_t R1
     if (x < R0) {
         sincos((double)(x - R0 / 2) * slope[f * 2 + 0], &s, &c);
         ex[f * R0 + x] = make_float2((float)c, (float)s);
+        ex64[f * R0 + x] = make_double2(c, s);
     } else {
         sincos((double)(x - R0 - R1 / 2) * slope[f * 2 + 1], &s, &c);
         ey[f * R1 + (x - R0)] = make_float2((float)c, (float)s);
+        ey64[f * R1 + (x - R0)] = make_double2(c, s);
     }
 }
 
-// nrm[f][cf][ou][ov] = sum over the CF's support of table * phase (FP64);
-// centre_only: only the zero offset (the weight grid's taps)
-__global__ void k_norms(const double *ck, const int32_t *support, const double *slope, int nf, int64_t ncf,
-                        int64_t R0, int64_t R1, int os0, int os1, int centre_only, double2 *nrm) {
+// nrm[f][cf][ou][ov] = sum over the CF's support of table * phase (FP64; the
+// phase exp(i(x px + y py)) = ex[x] ey[y]); centre_only: the zero offset only
+// (the weight grid's taps)
+__global__ void k_norms(const double *ck, const int32_t *support, const double2 *ex64, const double2 *ey64, int nf,
+                        int64_t ncf, int64_t R0, int64_t R1, int os0, int os1, int centre_only, double2 *nrm) {
     const int64_t no = centre_only ? 1 : (int64_t)(os0 + 1) * (os1 + 1);
     const int64_t id = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
     if (id >= nf * ncf * no) return;
@@ -112,208 +150,24 @@ __global__ void k_norms(const double *ck, const int32_t *support, const double *
     double re = 0.0, im = 0.0;
     for (int iv = -(sv / 2); iv < sv - sv / 2; ++iv) {
         const int64_t y = (int64_t)os1 * iv + ov + R1 / 2;
+        if (y < 0 || y >= R1) continue;
+        const double2 e = ey64[f * R1 + y];
+        double rr = 0.0, ri = 0.0;   // sum over x of k * ex[x]
         for (int iu = -(su / 2); iu < su - su / 2; ++iu) {
             const int64_t x = (int64_t)os0 * iu + ou + R0 / 2;
-            if (x < 0 || x >= R0 || y < 0 || y >= R1) continue;
+            if (x < 0 || x >= R0) continue;
             const double k = ck[(cf * R0 + x) * R1 + y];
-            double s, c;
-            sincos((double)(x - R0 / 2) * slope[f * 2] + (double)(y - R1 / 2) * slope[f * 2 + 1], &s, &c);
-            re += k * c;
-            im += k * s;
+            const double2 q = ex64[f * R0 + x];
+            rr += k * q.x;
+            ri += k * q.y;
         }
+        re += rr * e.x - ri * e.y;
+        im += rr * e.y + ri * e.x;
     }
     nrm[id] = make_double2(re, im);
 }
 
-struct GArgs {
-    const float2 *vis;
-    const float *weight;
-    const double *uvw;
-    const float4 *uvs;
-    const GChan *chan;
-    const int32_t *field_index, *cfb_map, *cfc_map, *cfp_map;
-    const float *ckr;
-    const float2 *ex, *ey;
-    const double2 *nrm;
-    float2 *grid;
-    double *sum_weight;
-    int64_t T, B, C, P, nu, nv, ncfb, ncfc, ncfp, ncf, R0, R1;
-    int os0, os1, S, maxsup, nk, n_img, continuum, fftl, nf;
-};
 
-template <bool DATA, bool FFTL, int KS>
-__global__ void __launch_bounds__(128) k_grid_gcf(const GArgs a) {
-    const int lane = threadIdx.x & 31;
-    const int64_t item = (int64_t)blockIdx.x * (blockDim.x >> 5) + (threadIdx.x >> 5);
-    if (item >= a.C * a.B * a.nk * a.P) return;
-    const int p = (int)(item % a.P);
-    const int64_t k = (item / a.P) % a.nk;
-    const int64_t b = (item / (a.P * a.nk)) % a.B;
-    const int64_t c = item / (a.P * a.nk * a.B);
-    const int64_t cimg = a.continuum ? 0 : c;
-    const int cfb = a.cfb_map[b], cfc = a.cfc_map[c], cfp = a.cfp_map[p];
-    if (cfb < 0 || cfb >= a.ncfb || cfc < 0 || cfc >= a.ncfc || cfp < 0 || cfp >= a.ncfp) return;
-    const int64_t cf = ((int64_t)cfb * a.ncfc + cfc) * a.ncfp + cfp;
-    const GChan cp = a.chan[c];
-    const int S = a.S, sc = S / 2;
-    const int cu_c = (int)(a.nu / 2), cv_c = (int)(a.nv / 2);
-    float2 *plane = a.grid + (cimg * a.P + p) * a.nu * a.nv;
-
-    // ---- producer: one visibility per lane ----
-    const int64_t t = k * GCH + lane;
-    unsigned cuv = 0, oo = 0;
-    int fidx = -1;
-    float2 wd = make_float2(0.f, 0.f);
-    double swl = 0.0;
-    if (t < a.T) {
-        const int64_t row = t * a.B + b;
-        fidx = a.field_index[row];
-        const float4 us = a.uvs[row];
-        if (fidx >= 0 && fidx < a.nf && !isnan(us.x) && !isnan(us.z)) {
-            int cu, ou, cv, ov;
-            if (!cell_pair(us.x, us.y, cp.suh, cp.sul, false, cu_c, a.os0, cu, ou)) {
-                long long i64, o64;
-                cell_fp64(a.uvw[row * 3 + 0], cp.su, false, cu_c, a.os0, i64, o64);
-                cu = (int)max(min(i64, (long long)1 << 30), -((long long)1 << 30));
-                ou = (int)o64;
-            }
-            if (!cell_pair(us.z, us.w, cp.svh, cp.svl, false, cv_c, a.os1, cv, ov)) {
-                long long i64, o64;
-                cell_fp64(a.uvw[row * 3 + 1], cp.sv, false, cv_c, a.os1, i64, o64);
-                cv = (int)max(min(i64, (long long)1 << 30), -((long long)1 << 30));
-                ov = (int)o64;
-            }
-            if (cu + a.maxsup < a.nu && cv + a.maxsup < a.nv && cu - a.maxsup >= 0 && cv - a.maxsup >= 0) {
-                const int64_t base = (row * a.C + c) * a.P + p;
-                const float w = a.weight[base];
-                bool ok;
-                if (DATA) {
-                    const float2 v = a.vis[base];
-                    wd = make_float2(v.x * w, v.y * w);
-                    ok = !isnan(wd.x) && !isnan(wd.y) && (wd.x != 0.f || wd.y != 0.f);
-                } else {
-                    wd = make_float2(w, 0.f);
-                    ok = !isnan(w) && w != 0.f;
-                }
-                const int oui = ou + a.os0 / 2, ovi = ov + a.os1 / 2;
-                ok = ok && oui >= 0 && oui <= a.os0 && ovi >= 0 && ovi <= a.os1;
-                if (ok) {
-                    cuv = ((unsigned)cu << 16) | (unsigned)cv;
-                    oo = 1u | ((unsigned)oui << 1) | ((unsigned)ovi << 12);
-                    const double2 n = a.nrm[((int64_t)fidx * a.ncf + cf) * (a.os0 + 1) * (a.os1 + 1) +
-                                            (int64_t)oui * (a.os1 + 1) + ovi];
-                    swl = DATA ? (double)w * (n.x * n.x - n.y * n.y) : (double)w * n.x;
-                }
-            }
-        }
-    }
-
-    // ---- consumer: the warp walks the chunk; lane = column class ----
-    float2 acc[KS];
-#pragma unroll
-    for (int i = 0; i < KS; ++i) acc[i] = make_float2(0.f, 0.f);
-    int prev_cu = -(1 << 28), prev_cv = -(1 << 28), mycol = -(1 << 28);
-    const bool active = lane < S;
-
-    // rows are residue classes too: class i sits on row row_of(i, cv)
-    auto row_of = [&](int i, int c) {
-        int m = (i - (c - sc)) % S;
-        m = m < 0 ? m + S : m;
-        return c - sc + m;
-    };
-    auto flushv = [&](float2 x, int row) {
-        if (x.x == 0.f && x.y == 0.f) return;
-        int u = mycol, v = row;
-        if (u < 0 || u >= a.nu || v < 0 || v >= a.nv) return;
-        if (FFTL) {
-            u = u < cu_c ? u + ((int)a.nu - cu_c) : u - cu_c;
-            v = v < cv_c ? v + ((int)a.nv - cv_c) : v - cv_c;
-        }
-        float *q = reinterpret_cast<float *>(plane + (int64_t)u * a.nv + v);
-        atomicAdd(q, x.x);
-        atomicAdd(q + 1, x.y);
-    };
-
-    for (int s = 0; s < GCH; ++s) {
-        const unsigned oos = __shfl_sync(0xffffffffu, oo, s);
-        if (!(oos & 1u)) continue;
-        const unsigned cuvs = __shfl_sync(0xffffffffu, cuv, s);
-        const int fs = __shfl_sync(0xffffffffu, fidx, s);
-        const float wdx = __shfl_sync(0xffffffffu, wd.x, s);
-        const float wdy = __shfl_sync(0xffffffffu, wd.y, s);
-        const int cu = (int)(cuvs >> 16), cv = (int)(cuvs & 0xffffu);
-        const int oui = (int)((oos >> 1) & 2047u), ovi = (int)((oos >> 12) & 2047u);
-        if (!active) continue;
-        if (cu != prev_cu) {
-            int m = (lane - (cu - sc)) % S;
-            m = m < 0 ? m + S : m;
-            const int nc = cu - sc + m;
-            if (nc != mycol) {
-#pragma unroll
-                for (int i = 0; i < KS; ++i) {
-                    if (i < S) flushv(acc[i], row_of(i, prev_cv));
-                    acc[i] = make_float2(0.f, 0.f);
-                }
-                mycol = nc;
-            }
-            prev_cu = cu;
-        }
-        if (cv != prev_cv) {
-            const int d = cv - prev_cv;
-            if (d == 1 || d == -1) {
-                const int ro = d > 0 ? prev_cv - sc : prev_cv + sc;   // the row leaving the window
-                int cls = ro % S;
-                cls = cls < 0 ? cls + S : cls;
-#pragma unroll
-                for (int i = 0; i < KS; ++i) {
-                    if (i == cls) {
-                        flushv(acc[i], ro);
-                        acc[i] = make_float2(0.f, 0.f);
-                    }
-                }
-            } else {
-#pragma unroll
-                for (int i = 0; i < KS; ++i) {
-                    if (i < S) {
-                        const int ro = row_of(i, prev_cv);
-                        if (ro != row_of(i, cv)) {
-                            flushv(acc[i], ro);
-                            acc[i] = make_float2(0.f, 0.f);
-                        }
-                    }
-                }
-            }
-            prev_cv = cv;
-        }
-        const int du = mycol - cu;   // in [-sc, sc]
-        const float *blk = a.ckr + ((((cf * (a.os0 + 1) + oui) * (a.os1 + 1) + ovi) * S) + (du + sc)) * SP;
-        const int ou = oui - a.os0 / 2, ov = ovi - a.os1 / 2;
-        const float2 exv = a.ex[(int64_t)fs * a.R0 + a.os0 * du + ou + a.R0 / 2];
-        const float2 A = make_float2(exv.x * wdx - exv.y * wdy, exv.x * wdy + exv.y * wdx);
-        const float2 *eyr = a.ey + (int64_t)fs * a.R1 + ov + a.R1 / 2 - a.os1 * sc;
-        int m = (cv - sc) % S;
-        m = m < 0 ? m + S : m;
-#pragma unroll
-        for (int i = 0; i < KS; ++i) {
-            if (i < S) {
-                int dd = i - m;            // tap index (dv + sc) of row class i
-                dd += dd < 0 ? S : 0;
-                const float kk = __ldg(blk + dd);
-                const float2 e = __ldg(eyr + a.os1 * dd);
-                const float br = A.x * e.x - A.y * e.y, bi = A.x * e.y + A.y * e.x;
-                acc[i].x = fmaf(kk, br, acc[i].x);
-                acc[i].y = fmaf(kk, bi, acc[i].y);
-            }
-        }
-    }
-    if (active) {
-#pragma unroll
-        for (int i = 0; i < KS; ++i)
-            if (i < S) flushv(acc[i], row_of(i, prev_cv));
-    }
-    for (int o = 16; o > 0; o >>= 1) swl += __shfl_xor_sync(0xffffffffu, swl, o);
-    if (lane == 0 && swl != 0.0) atomicAdd(a.sum_weight + cimg * a.P + p, swl);
-}
 
 // ---- mosaic weight grid ----------------------------------------------------
 // wsum[cimg][p][f][cfb][cfc] = sum of weights of the rows that pass the edge rule
@@ -352,7 +206,7 @@ __global__ void k_wsum(const GArgs a, int64_t nfb, double *wsum) {
 }
 
 // weight-grid patch at the grid centre and its sum_weight
-__global__ void k_wpatch(const GArgs a, const double *wk, const int32_t *support, const double *slope, int nf,
+__global__ void k_wpatch(const GArgs a, const double *wk, const int32_t *support, int nf,
                          int64_t ncfb, const double *wsum, const double2 *nrm_w) {
     const int64_t id = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
     const int S = a.S, sc = S / 2;
@@ -360,7 +214,6 @@ __global__ void k_wpatch(const GArgs a, const double *wk, const int32_t *support
     if (id >= (int64_t)a.n_img * a.P * per) return;
     const int64_t q = id / per;   // cimg * P + p
     const int p = (int)(q % a.P);
-    const int64_t cimg = q / a.P;
     const int iu = (int)((id % per) / S) - sc, iv = (int)(id % S) - sc;
     const int cfp = a.cfp_map[p];
     if (cfp < 0 || cfp >= a.ncfp) return;
@@ -375,8 +228,8 @@ __global__ void k_wpatch(const GArgs a, const double *wk, const int32_t *support
                 if (!in_support(iu, support[cf * 2]) || !in_support(iv, support[cf * 2 + 1])) continue;
                 const int64_t x = (int64_t)a.os0 * iu + a.R0 / 2, y = (int64_t)a.os1 * iv + a.R1 / 2;
                 const double kk = wk[(cf * a.R0 + x) * a.R1 + y];
-                double s, c;
-                sincos((double)(x - a.R0 / 2) * slope[f * 2] + (double)(y - a.R1 / 2) * slope[f * 2 + 1], &s, &c);
+                const double2 ex = a.ex64[(int64_t)f * a.R0 + x], ey = a.ey64[(int64_t)f * a.R1 + y];
+                const double c = ex.x * ey.x - ex.y * ey.y, s = ex.x * ey.y + ex.y * ey.x;
                 re += w * kk * c;
                 im += w * kk * s;
             }
@@ -527,25 +380,37 @@ int gcf_setup(const NggGcfArgs *a, cudaStream_t s, GScratch &sc, GArgs &g, int *
     int rc;
     GChan *chan = nullptr;
     float4 *uvs = nullptr;
-    float *ckr = nullptr;
+    float *ckt = nullptr;
+    float2 *gx = nullptr, *gy = nullptr, *hx = nullptr, *hy = nullptr;
     float2 *ex = nullptr, *ey = nullptr;
+    double2 *ex64 = nullptr, *ey64 = nullptr;
     double2 *nrm = nullptr;
     if ((rc = sc.get((void **)&chan, sizeof(GChan) * (C > 0 ? C : 1))) != NGG_OK) return rc;
     if ((rc = sc.get((void **)&uvs, sizeof(float4) * (T * B > 0 ? T * B : 1))) != NGG_OK) return rc;
-    const int64_t nck = ncf * (a->oversampling[0] + 1) * (a->oversampling[1] + 1) * S * SP;
-    if ((rc = sc.get((void **)&ckr, sizeof(float) * nck)) != NGG_OK) return rc;
+    const int64_t nck = ncf * (a->oversampling[0] + 1) * (a->oversampling[1] + 1) * 2 * S * SP;
+    if ((rc = sc.get((void **)&ckt, sizeof(float) * nck)) != NGG_OK) return rc;
+    const int64_t nf = a->n_field;
+    if ((rc = sc.get((void **)&gx, sizeof(float2) * nf * a->n_u)) != NGG_OK) return rc;
+    if ((rc = sc.get((void **)&gy, sizeof(float2) * nf * a->n_v)) != NGG_OK) return rc;
+    if ((rc = sc.get((void **)&hx, sizeof(float2) * nf * (a->oversampling[0] + 1))) != NGG_OK) return rc;
+    if ((rc = sc.get((void **)&hy, sizeof(float2) * nf * (a->oversampling[1] + 1))) != NGG_OK) return rc;
     if ((rc = sc.get((void **)&ex, sizeof(float2) * a->n_field * a->conv_size[0])) != NGG_OK) return rc;
     if ((rc = sc.get((void **)&ey, sizeof(float2) * a->n_field * a->conv_size[1])) != NGG_OK) return rc;
+    if ((rc = sc.get((void **)&ex64, sizeof(double2) * a->n_field * a->conv_size[0])) != NGG_OK) return rc;
+    if ((rc = sc.get((void **)&ey64, sizeof(double2) * a->n_field * a->conv_size[1])) != NGG_OK) return rc;
     const int64_t nn = a->n_field * ncf * (a->oversampling[0] + 1) * (a->oversampling[1] + 1);
     if ((rc = sc.get((void **)&nrm, sizeof(double2) * nn)) != NGG_OK) return rc;
     if (C > 0) k_gchan<<<(unsigned)((C + 127) / 128), 128, 0, s>>>(a->freq, (int)C, a->delta_lm[0], a->delta_lm[1], a->n_u, a->n_v, chan);
     if (T * B > 0) k_gsplit<<<(unsigned)((T * B + 255) / 256), 256, 0, s>>>(a->uvw, T * B, uvs);
     k_reorg<<<(unsigned)((nck + 255) / 256), 256, 0, s>>>(a->conv_kernel, ncf, a->conv_size[0], a->conv_size[1],
-                                                         a->oversampling[0], a->oversampling[1], a->support, S, ckr);
+                                                         a->oversampling[0], a->oversampling[1], a->support, S, ckt);
+    const int64_t ncp = nf * (a->n_u + a->n_v + a->oversampling[0] + 1 + a->oversampling[1] + 1);
+    k_cell_phase<<<(unsigned)((ncp + 255) / 256), 256, 0, s>>>(a->phase_slope, a->n_field, a->n_u, a->n_v,
+                                                              a->oversampling[0], a->oversampling[1], gx, gy, hx, hy);
     const int64_t npt = (int64_t)a->n_field * (a->conv_size[0] + a->conv_size[1]);
     k_phase_tabs<<<(unsigned)((npt + 255) / 256), 256, 0, s>>>(a->phase_slope, a->n_field, a->conv_size[0],
-                                                              a->conv_size[1], ex, ey);
-    k_norms<<<(unsigned)((nn + 127) / 128), 128, 0, s>>>(a->conv_kernel, a->support, a->phase_slope, a->n_field, ncf,
+                                                              a->conv_size[1], ex, ey, ex64, ey64);
+    k_norms<<<(unsigned)((nn + 127) / 128), 128, 0, s>>>(a->conv_kernel, a->support, ex64, ey64, a->n_field, ncf,
                                                         a->conv_size[0], a->conv_size[1], a->oversampling[0],
                                                         a->oversampling[1], 0, nrm);
     NGG_CHECK_LAUNCH("gcf set-up kernels");
@@ -558,9 +423,12 @@ int gcf_setup(const NggGcfArgs *a, cudaStream_t s, GScratch &sc, GArgs &g, int *
     g.cfb_map = a->cf_baseline_map;
     g.cfc_map = a->cf_chan_map;
     g.cfp_map = a->cf_pol_map;
-    g.ckr = ckr;
+    g.ckt = ckt;
+    g.gx = gx; g.gy = gy; g.hx = hx; g.hy = hy;
     g.ex = ex;
     g.ey = ey;
+    g.ex64 = ex64;
+    g.ey64 = ey64;
     g.nrm = nrm;
     g.grid = (float2 *)a->grid;
     g.sum_weight = a->sum_weight;
@@ -601,16 +469,9 @@ extern "C" int ngg_grid_gcf(const NggGcfArgs *a, void *stream) {
     if ((rc = gcf_setup(a, s, sc, g, &S)) != NGG_OK) return rc;
     const int64_t items = a->n_chan * a->n_baseline * g.nk * a->n_pol;
     const unsigned blocks = (unsigned)((items + 3) / 4);
-    const bool fftl = a->layout == NGG_LAYOUT_FFT, data = a->mode == NGG_MODE_DATA;
-    if (S <= 15) {
-        if (data) (fftl ? k_grid_gcf<true, true, 15> : k_grid_gcf<true, false, 15>)<<<blocks, 128, 0, s>>>(g);
-        else (fftl ? k_grid_gcf<false, true, 15> : k_grid_gcf<false, false, 15>)<<<blocks, 128, 0, s>>>(g);
-    } else {
-        if (data) (fftl ? k_grid_gcf<true, true, MAXS> : k_grid_gcf<true, false, MAXS>)<<<blocks, 128, 0, s>>>(g);
-        else (fftl ? k_grid_gcf<false, true, MAXS> : k_grid_gcf<false, false, MAXS>)<<<blocks, 128, 0, s>>>(g);
-    }
-    NGG_CHECK_LAUNCH("k_grid_gcf");
-    return NGG_OK;
+    const bool data = a->mode == NGG_MODE_DATA;
+    if (S <= 15) return launch_grid_gcf_lo(g, data, blocks, s);
+    return S <= 23 ? launch_grid_gcf_mid(g, data, blocks, s) : launch_grid_gcf_hi(g, data, blocks, s);
 }
 
 extern "C" int ngg_grid_gcf_weight(const NggGcfArgs *a, void *stream) {
@@ -636,13 +497,13 @@ extern "C" int ngg_grid_gcf_weight(const NggGcfArgs *a, void *stream) {
     const int64_t nnw = (int64_t)a->n_field * g.ncf;
     if ((rc = sc.get((void **)&nrm_w, sizeof(double2) * nnw)) != NGG_OK) return rc;
     NGG_CUDA(cudaMemsetAsync(wsum, 0, sizeof(double) * nws, s));
-    k_norms<<<(unsigned)((nnw + 127) / 128), 128, 0, s>>>(a->conv_kernel, a->support, a->phase_slope, a->n_field, g.ncf,
+    k_norms<<<(unsigned)((nnw + 127) / 128), 128, 0, s>>>(a->conv_kernel, a->support, g.ex64, g.ey64, a->n_field, g.ncf,
                                                          a->conv_size[0], a->conv_size[1], a->oversampling[0],
                                                          a->oversampling[1], 1, nrm_w);
     const int64_t n = a->n_time * a->n_baseline * a->n_chan;
     k_wsum<<<(unsigned)((n + 255) / 256), 256, 0, s>>>(g, a->n_field, wsum);
     const int64_t np = n_img * a->n_pol * (int64_t)S * S;
-    k_wpatch<<<(unsigned)((np + 127) / 128), 128, 0, s>>>(g, a->conv_kernel, a->support, a->phase_slope, a->n_field,
+    k_wpatch<<<(unsigned)((np + 127) / 128), 128, 0, s>>>(g, a->conv_kernel, a->support, a->n_field,
                                                          ncfb, wsum, nrm_w);
     NGG_CHECK_LAUNCH("ngg_grid_gcf_weight kernels");
     return NGG_OK;

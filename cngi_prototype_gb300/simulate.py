@@ -243,3 +243,124 @@ def config_large_cube(seed=2, n_time=1024, n_chan=256, vis_device=None, with_vis
     return make_observation(64, 'log_spiral', 2500.0, n_time, 8.0, freq, 2, 200, (1e-3, 1.0),
                             fov, 0.05, (4096, 4096), (1.0, 1.0), seed, flag_fraction=0.05,
                             flux_law='power', vis_device=vis_device, with_vis=with_vis)
+
+
+# ---------------------------------------------------------------------------
+# mosaic observations
+# ---------------------------------------------------------------------------
+def sin_to_radec(l, m, phase_center):
+    """Inverse SIN (orthographic) projection: direction cosines (l, m) about
+    phase_center (ra0, dec0) -> (ra, dec) in radians."""
+    a0, d0 = phase_center
+    n = np.sqrt(1.0 - l ** 2 - m ** 2)
+    dec = np.arcsin(m * np.cos(d0) + n * np.sin(d0))
+    ra = a0 + np.arctan2(l, n * np.cos(d0) - m * np.sin(d0))
+    return ra, dec
+
+
+def hex_offsets(n, spacing):
+    """n points of a hexagonal grid of the given spacing, nearest the origin first."""
+    k = int(np.ceil(np.sqrt(n))) + 2
+    pts = []
+    for j in range(-k, k + 1):
+        for i in range(-k, k + 1):
+            pts.append(((i + 0.5 * (j % 2)) * spacing, j * spacing * np.sqrt(3) / 2))
+    pts = np.array(pts)
+    pts = pts - pts[np.argmin(np.hypot(pts[:, 0], pts[:, 1]))]
+    order = np.lexsort((np.arctan2(pts[:, 1], pts[:, 0]), np.round(np.hypot(pts[:, 0], pts[:, 1]) / spacing, 6)))
+    return pts[order[:n]]
+
+
+def casa_airy_voltage(r, freq, dish, blockage):
+    """CASA obscured-aperture Airy voltage pattern at angle r (radians)."""
+    from scipy.special import j1
+    x = np.asarray(r) * (2 * np.pi * freq / C_LIGHT) * dish / 2
+    x = np.where(x == 0, 1e-30, x)
+    if blockage == 0:
+        return 2 * j1(x) / x
+    A, L = (dish / blockage) ** 2, dish / blockage
+    return (A * 2 * j1(x) / x - 2 * j1(x * L) / (x * L)) / (A - 1.0)
+
+
+def config_mosaic(seed=4, n_chan=16, n_int=30, n_pointing=49, n_comp=300, n_pol=2, vis_device='cuda',
+                  n_ant=50, radius_m=750.0, dt_s=6.0):
+    """Mosaic aperture-projection workload: 50 x 12 m antennas (0.75 m
+    blockage, CASA Airy) uniform in a 750 m-radius disk (1225 baselines),
+    49 pointings on a hexagonal grid at half-beam spacing (FWHM 1.02 lambda/D
+    at 100.8 GHz), 30 integrations of 6 s per pointing (1470 times), 16
+    channels over 100-101.6 GHz, RR/LL, a sky of 300 Gaussian components
+    (flux U[0.05, 1] Jy, FWHM U[0.2, 2] arcsec) spread over the mosaic, noise
+    sigma 0.05 Jy. 2048^2 image at 0.2 arcsec, GCF oversampling 20, max
+    support 31.
+
+    Each visibility is V = sum_k S_k P_f(k) exp(-2 pi^2 s_k^2 |uv|^2)
+    exp(+2 pi i (u l_k + v m_k)): the sign puts a component at direction
+    (l, m) at the image pixel the reference's SIN WCS gives that direction,
+    pixel offset (l / cell0, m / cell1) with cell0 < 0 -- the pixel where
+    make_mosaic_pb places a pointing in that direction. P_f = the baseline's
+    primary beam (voltage pattern squared) of the row's pointing f at the
+    component. Data are in the common phase-centre frame (as after
+    direction_rotate). Returns an Observation; vis / weight are CUDA tensors
+    when vis_device is set.
+    """
+    rng = np.random.default_rng(seed)
+    dish, block = 12.0, 0.75
+    enu = disk_layout(n_ant, radius_m, rng)
+    T = n_int * n_pointing
+    uvw = earth_rotation_uvw(enu, T, dt_s)
+    B = uvw.shape[1]
+    a1, a2 = baseline_pairs(n_ant)
+    freq = 100.0e9 + (np.arange(n_chan) + 0.5) * (1.6e9 / n_chan)
+    fwhm = 1.02 * (C_LIGHT / 100.8e9) / dish
+    pc = np.array([np.deg2rad(150.0), np.deg2rad(45.0)])
+    off = hex_offsets(n_pointing, fwhm / 2)                        # (l, m) of each pointing
+    ra, dec = sin_to_radec(off[:, 0], off[:, 1], pc)
+    field_phase_dir = np.stack([ra, dec], axis=1)
+    extent = np.abs(off).max(axis=0) + fwhm / 2
+    cl = rng.uniform(-extent[0], extent[0], n_comp)
+    cm = rng.uniform(-extent[1], extent[1], n_comp)
+    flux = rng.uniform(0.05, 1.0, n_comp)
+    sig = np.deg2rad(rng.uniform(0.2, 2.0, n_comp) / 3600) / (2 * np.sqrt(2 * np.log(2)))
+    field = np.repeat(np.arange(n_pointing), n_int)[:, None].repeat(B, axis=1).astype(np.int32)
+    # primary-beam gain of every (pointing, component, channel)
+    dist = np.hypot(cl[None, :] - off[:, 0:1], cm[None, :] - off[:, 1:2])
+    pbg = np.stack([casa_airy_voltage(dist, f, dish, block) ** 2 for f in freq], axis=-1)   # (F, K, C)
+    obs = Observation(uvw=uvw, freq=freq, field=field, field_phase_dir=field_phase_dir, phase_center=pc,
+                      antenna1=a1, antenna2=a2, pointing_lm=off, comp_lm=np.stack([cl, cm], 1), comp_flux=flux,
+                      comp_sigma=sig, image_size=[2048, 2048], cell_arcsec=[0.2, 0.2], dish=dish, blockage=block,
+                      oversampling=[20, 20], max_support=[31, 31])
+    if vis_device is None:
+        return obs
+    import torch
+    dev = torch.device(vis_device)
+    u = torch.as_tensor(uvw[..., 0].reshape(-1), device=dev, dtype=torch.float64)
+    v = torch.as_tensor(uvw[..., 1].reshape(-1), device=dev, dtype=torch.float64)
+    fr = torch.as_tensor(field.reshape(-1), device=dev, dtype=torch.int64)
+    lt = torch.as_tensor(cl, device=dev, dtype=torch.float64)
+    mt = torch.as_tensor(cm, device=dev, dtype=torch.float64)
+    s2 = torch.as_tensor(2 * np.pi ** 2 * sig ** 2, device=dev, dtype=torch.float64)
+    amp = torch.as_tensor(flux[None, :, None] * pbg, device=dev, dtype=torch.float32)      # (F, K, C)
+    gen = torch.Generator(device=dev)
+    gen.manual_seed(int(seed) + 4000)
+    vis = torch.empty((T * B, n_chan, n_pol), dtype=torch.complex64, device=dev)
+    rows_per = max(1, (1 << 26) // n_comp)
+    for r0 in range(0, T * B, rows_per):
+        r1 = min(T * B, r0 + rows_per)
+        base = (u[r0:r1, None] * lt[None, :] + v[r0:r1, None] * mt[None, :]) / C_LIGHT      # turns per Hz
+        q2 = (u[r0:r1] ** 2 + v[r0:r1] ** 2) / C_LIGHT ** 2                                  # (uv / lambda)^2 per Hz^2
+        for c in range(n_chan):
+            a = amp[:, :, c][fr[r0:r1]]                                                       # (rows, K)
+            f = float(freq[c])
+            turns = base * f
+            turns = turns - torch.round(turns)
+            ph = (turns * (2 * np.pi)).float()
+            g = torch.exp(-(q2[:, None] * f * f) * s2[None, :]).float() * a
+            re = (torch.cos(ph) * g).sum(-1)
+            im = (torch.sin(ph) * g).sum(-1)
+            for p in range(n_pol):
+                nr = 0.05 * torch.randn(r1 - r0, generator=gen, device=dev)
+                ni = 0.05 * torch.randn(r1 - r0, generator=gen, device=dev)
+                vis[r0:r1, c, p] = torch.complex(re + nr, im + ni)
+    obs['vis'] = vis.view(T, B, n_chan, n_pol)
+    obs['weight'] = torch.ones((T, B, n_chan, n_pol), dtype=torch.float32, device=dev)
+    return obs

@@ -36,6 +36,10 @@ def lib():
         L.ngg_oracle_weight_degrid.argtypes = [P, P, P, P, i64, i64, i64, i64, P, P, P, ctypes.c_int,
                                                ctypes.c_int, P]
         L.ngg_oracle_weight_degrid.restype = ctypes.c_int
+        L.ngg_oracle_aperture_grid.argtypes = [ctypes.c_int, P, P, P, P, i64, i64, i64, i64, P, P, P, P, i64, i64,
+                                               i64, P, P, P, i64, i64, i64, P, P, P, ctypes.c_int, ctypes.c_int,
+                                               P, P]
+        L.ngg_oracle_aperture_grid.restype = ctypes.c_int
         _lib = L
     return _lib
 
@@ -89,3 +93,39 @@ def weight_degrid(density_uvcp, uvw, weight, briggs, freq, n_uv, delta_lm, chan_
     if rc != 0:
         raise RuntimeError('ngg_oracle_weight_degrid failed')
     return out
+
+
+APERTURE_KINDS = {'data': 0, 'psf': 1, 'weight': 2}
+
+
+def aperture_grid(kind, vis, uvw, imaging_weight, field_index, cf_baseline_map, cf_chan_map, cf_pol_map, table,
+                  support, phase_gradient, freq, oversampling, n_uv, delta_lm, chan_mode='cube', n_threads=0):
+    """Mosaic gridders in FP64 (_aperture_grid_jit / _aperture_weight_grid_jit).
+    field_index: (T, B) index into the phase-gradient planes, < 0 skips.
+    Returns (grid complex128 (Cimg, P, Nu, Nv), sum_weight (Cimg, P))."""
+    i64 = np.int64
+    uvw = np.ascontiguousarray(uvw, dtype=np.float64)
+    w = np.ascontiguousarray(imaging_weight, dtype=np.float64)
+    T, B, C, P = w.shape
+    v = np.ascontiguousarray(vis, dtype=np.complex64) if kind == 'data' else None
+    fidx = np.ascontiguousarray(field_index, dtype=i64)
+    maps = [np.ascontiguousarray(m, dtype=i64) for m in (cf_baseline_map, cf_chan_map, cf_pol_map)]
+    tab = np.ascontiguousarray(table, dtype=np.float64)
+    sup = np.ascontiguousarray(support, dtype=i64)
+    pg = np.ascontiguousarray(phase_gradient, dtype=np.complex128)
+    os_ = np.ascontiguousarray(oversampling, dtype=i64)
+    nuv = np.ascontiguousarray(n_uv, dtype=i64)
+    dl = np.ascontiguousarray(delta_lm, dtype=np.float64)
+    f = np.ascontiguousarray(freq, dtype=np.float64)
+    cont = 1 if chan_mode == 'continuum' else 0
+    n_img = 1 if cont else C
+    g = np.empty((n_img, P, int(nuv[0]), int(nuv[1])), dtype=np.complex128)
+    sw = np.empty((n_img, P), dtype=np.float64)
+    ncfb, ncfc, ncfp, R0, R1 = tab.shape
+    rc = lib().ngg_oracle_aperture_grid(APERTURE_KINDS[kind], _p(v), _p(uvw), _p(w), _p(fidx), T, B, C, P, _p(f),
+                                        _p(maps[0]), _p(maps[1]), _p(maps[2]), ncfb, ncfc, ncfp, _p(tab), _p(sup),
+                                        _p(pg), pg.shape[0], R0, R1, _p(os_), _p(nuv), _p(dl), cont,
+                                        int(n_threads), _p(g), _p(sw))
+    if rc != 0:
+        raise RuntimeError('ngg_oracle_aperture_grid failed')
+    return g, sw

@@ -243,3 +243,124 @@ int ngg_oracle_weight_degrid(const double *density, const double *uvw, const dou
     free(sv);
     return 0;
 }
+
+/* ------------------------------------------------------------------------
+ * Mosaic gridders, restating loop for loop
+ *   _aperture_grid_jit          ngcasa/imaging/_imaging_utils/_aperture_grid.py:376-513
+ *   _aperture_weight_grid_jit   _aperture_grid.py:180-291
+ * conv = table[cfb,cfc,cfp,x,y] * phase_gradient[field,x,y] evaluated as
+ * (k*pr, k*pi); addend = conv * weighted_data with the scalar complex
+ * formula; norm summed in tap order; sum_weight += w*Re(norm^2) (data) or
+ * w*Re(norm) (psf, weight).  Cube mode runs channels in parallel (each
+ * channel's cells and sums receive their addends in the reference order);
+ * continuum mode is sequential.
+ *   kind: 0 data, 1 psf, 2 weight grid (taps at the grid centre, zero offset)
+ *   field_index (T,B): index into the phase-gradient planes, < 0 skips the row
+ *   table (ncfb,ncfc,ncfp,R0,R1) f64; support (ncfb,ncfc,ncfp,2) int64;
+ *   pg (n_field,R0,R1) complex128; grid complex128 (Cimg,P,Nu,Nv).
+ * ------------------------------------------------------------------------ */
+static void aperture_block(int kind, const float *vis, const double *uvw, const double *weight,
+                           const int64_t *field_index, int64_t T, int64_t B, int64_t C, int64_t P,
+                           int64_t c0, int64_t c1, int continuum, const double *su, const double *sv,
+                           const int64_t *cfb_map, const int64_t *cfc_map, const int64_t *cfp_map,
+                           int64_t ncfc, int64_t ncfp, const double *table, const int64_t *support,
+                           int64_t maxsup, const double *pg, int64_t R0, int64_t R1, const int64_t os[2],
+                           const int64_t n_uv[2], double *grid, double *sumw) {
+    const int64_t nu = n_uv[0], nv = n_uv[1], ucen = nu / 2, vcen = nv / 2;
+    const int64_t cc0 = R0 / 2, cc1 = R1 / 2;
+    for (int64_t t = 0; t < T; ++t) {
+        for (int64_t b = 0; b < B; ++b) {
+            const int64_t fi = field_index[t * B + b];
+            if (fi < 0) continue;
+            const int64_t cfb = cfb_map[b];
+            for (int64_t c = c0; c < c1; ++c) {
+                const int64_t cfc = cfc_map[c];
+                const int64_t ac = continuum ? 0 : c;
+                const double u = uvw[(t * B + b) * 3 + 0] * su[c];
+                const double v = uvw[(t * B + b) * 3 + 1] * sv[c];
+                if (isnan(u) || isnan(v)) continue;
+                const double up = u + (double)ucen, vp = v + (double)vcen;
+                const int64_t cu = (int64_t)(up + 0.5), cv = (int64_t)(vp + 0.5);
+                if (!(cu + maxsup < nu && cv + maxsup < nv && cu - maxsup >= 0 && cv - maxsup >= 0)) continue;
+                int64_t ou, ov, gu, gv;
+                if (kind == 2) {
+                    ou = cc0; ov = cc1; gu = ucen; gv = vcen;
+                } else {
+                    ou = (int64_t)floor(((double)cu - up) * (double)os[0] + 0.5) + cc0;
+                    ov = (int64_t)floor(((double)cv - vp) * (double)os[1] + 0.5) + cc1;
+                    gu = cu; gv = cv;
+                }
+                for (int64_t p = 0; p < P; ++p) {
+                    const int64_t vi = ((t * B + b) * C + c) * P + p;
+                    const double w = weight[vi];
+                    double wr, wi;
+                    if (kind == 0) {
+                        wr = (double)vis[2 * vi] * w;
+                        wi = (double)vis[2 * vi + 1] * w;
+                        if (isnan(wr) || isnan(wi) || (wr == 0.0 && wi == 0.0)) continue;
+                    } else {
+                        wr = w; wi = 0.0;
+                        if (isnan(w) || w == 0.0) continue;
+                    }
+                    const int64_t cfp = cfp_map[p];
+                    const int64_t cf = (cfb * ncfc + cfc) * ncfp + cfp;
+                    const int64_t s_u = support[cf * 2], s_v = support[cf * 2 + 1];
+                    double nr = 0.0, ni = 0.0;
+                    double *g = grid + 2 * ((ac * P + p) * nu * nv);
+                    for (int64_t iv = -(s_v / 2); iv < s_v - s_v / 2; ++iv) {
+                        const int64_t y = os[1] * iv + ov;
+                        for (int64_t iu = -(s_u / 2); iu < s_u - s_u / 2; ++iu) {
+                            const int64_t x = os[0] * iu + ou;
+                            const double k = table[(cf * R0 + x) * R1 + y];
+                            const double *ph = pg + 2 * ((fi * R0 + x) * R1 + y);
+                            const double cr = k * ph[0], ci = k * ph[1];
+                            const double ar = cr * wr - ci * wi, ai = cr * wi + ci * wr;
+                            double *cell = g + 2 * ((gu + iu) * nv + (gv + iv));
+                            cell[0] = cell[0] + ar;
+                            cell[1] = cell[1] + ai;
+                            nr = nr + cr;
+                            ni = ni + ci;
+                        }
+                    }
+                    double *s = sumw + ac * P + p;
+                    if (kind == 0) *s = *s + w * (nr * nr - ni * ni);
+                    else *s = *s + w * nr;
+                }
+            }
+        }
+    }
+}
+
+int ngg_oracle_aperture_grid(int kind, const float *vis, const double *uvw, const double *weight,
+                             const int64_t *field_index, int64_t T, int64_t B, int64_t C, int64_t P,
+                             const double *freq, const int64_t *cfb_map, const int64_t *cfc_map,
+                             const int64_t *cfp_map, int64_t ncfb, int64_t ncfc, int64_t ncfp,
+                             const double *table, const int64_t *support, const double *pg, int64_t n_field,
+                             int64_t R0, int64_t R1, const int64_t os[2], const int64_t n_uv[2],
+                             const double dl[2], int continuum, int n_threads, double *grid, double *sumw) {
+    (void)ncfb; (void)n_field;
+    const int64_t n_img = continuum ? 1 : C;
+    memset(grid, 0, sizeof(double) * 2 * (size_t)(n_img * P * n_uv[0] * n_uv[1]));
+    memset(sumw, 0, sizeof(double) * (size_t)(n_img * P));
+    if (T * B * C == 0) return 0;
+    double *su = malloc(sizeof(double) * C), *sv = malloc(sizeof(double) * C);
+    if (!su || !sv) { free(su); free(sv); return 1; }
+    uv_scale(freq, (int)C, dl, n_uv, su, sv);
+    int64_t maxsup = 0;
+    for (int64_t i = 0; i < ncfb * ncfc * ncfp * 2; ++i) maxsup = support[i] > maxsup ? support[i] : maxsup;
+    if (continuum) {
+        aperture_block(kind, vis, uvw, weight, field_index, T, B, C, P, 0, C, 1, su, sv, cfb_map, cfc_map, cfp_map,
+                       ncfc, ncfp, table, support, maxsup, pg, R0, R1, os, n_uv, grid, sumw);
+    } else {
+#ifdef _OPENMP
+        if (n_threads > 0) omp_set_num_threads(n_threads);
+#pragma omp parallel for schedule(dynamic, 1)
+#endif
+        for (int64_t c = 0; c < C; ++c)
+            aperture_block(kind, vis, uvw, weight, field_index, T, B, C, P, c, c + 1, 0, su, sv, cfb_map, cfc_map,
+                           cfp_map, ncfc, ncfp, table, support, maxsup, pg, R0, R1, os, n_uv, grid, sumw);
+    }
+    free(su);
+    free(sv);
+    return 0;
+}

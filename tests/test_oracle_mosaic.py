@@ -108,3 +108,27 @@ def test_product_host_logic_matches_oracle(gold):
     assert np.array_equal(_mosaic.field_indices(f, [7, 3]), [[1, 1, -1], [0, 1, 0]])
     with pytest.raises(ValueError):
         _mosaic.field_indices(f, [3])
+
+
+@pytest.mark.parametrize('tag', ['grid', 'psf_grid', 'weight_grid'])
+def test_c_aperture_oracle_matches_reference(gold, tag):
+    from oracle import cbind
+    d = gold
+    gp = _gp(d)
+    kind = {'grid': 'data', 'psf_grid': 'psf', 'weight_grid': 'weight'}[tag]
+    kern = d['weight_conv_kernel'] if tag == 'weight_grid' else d['conv_kernel']
+    fidx = np.where(d['field'] >= 0, d['field'], -1)
+    g, sw = cbind.aperture_grid(kind, d['vis'], d['uvw'], d['imaging_weight'], fidx, d['cf_baseline_map'],
+                                d['cf_chan_map'], d['cf_pol_map'], kern, d['support'], d['phase_gradient'], d['freq'],
+                                d['oversampling'], gp['image_size_padded'], gp['cell_size'])
+    swk = {'grid': 'sum_weight', 'psf_grid': 'psf_sum_weight', 'weight_grid': 'weight_sum_weight'}[tag]
+    assert np.array_equal(g, d[tag]) and np.array_equal(sw, d[swk])
+    gc, swc = cbind.aperture_grid(kind, d['vis'], d['uvw'], d['imaging_weight'], fidx, d['cf_baseline_map'],
+                                  d['cf_chan_map'], d['cf_pol_map'], kern, d['support'], d['phase_gradient'],
+                                  d['freq'], d['oversampling'], gp['image_size_padded'], gp['cell_size'],
+                                  chan_mode='continuum')
+    gn, swn = M.aperture_grid(d['vis'], d['uvw'], d['imaging_weight'], d['field'], np.arange(2), d['cf_baseline_map'],
+                              d['cf_chan_map'], d['cf_pol_map'], kern, d['support'], d['phase_gradient'], d['freq'],
+                              gp['image_size_padded'], gp['cell_size'], d['oversampling'], 'continuum',
+                              do_psf=kind == 'psf', weight_grid=kind == 'weight')
+    assert np.array_equal(gc, gn) and np.array_equal(swc, swn)

@@ -53,6 +53,9 @@ def parse():
                    help='large_cube (default, the headline) or mosaic (aperture-projection imaging, table GCF)')
     p.add_argument('--mosaic-chans', type=int, default=16)
     p.add_argument('--mosaic-pointings', type=int, default=49)
+    p.add_argument('--no-learned', action='store_true')
+    p.add_argument('--learned-steps', type=int, default=30000)
+    p.add_argument('--learned-freqs', type=int, default=64)
     return p.parse_args()
 
 
@@ -203,6 +206,89 @@ def _mosaic_mxds(obs, vis, weight, field_ds):
     return xds.mxds({'xds0': vds}, FIELD=field_ds)
 
 
+def _dirty(grid_fft, sw, chans):
+    """Re(FFT^-1) of FFT-layout planes / sum_weight for a few channels (numpy FP64)."""
+    out = []
+    for c in chans:
+        g = grid_fft[c].cpu().numpy().astype(np.complex128)
+        im = np.fft.fftshift(np.fft.ifft2(g), axes=(1, 2)).real
+        s = sw[c].cpu().numpy()
+        out.append(im / np.where(s == 0, 1.0, s)[:, None, None])
+    return np.stack(out)
+
+
+def learned_leg(args, obs, gcf, gp, vis_d, uvw_d, w_d, f_d, fidx_d, sl_d, g_tab, sw_tab, ms_tab, t_gcf):
+    """Learned GCF against the table GCF on the mosaic workload: train on the
+    GCFs the method generates (GPU), grid with per-channel tables synthesised
+    on the tensor cores, compare images with the table path (reference PB
+    channels) and with a table built at every channel's exact frequency."""
+    import torch
+    from cngi_prototype_gb300 import _lib
+    from cngi_prototype_gb300.imaging.learned_gcf import LearnedGCF
+    from cngi_prototype_gb300.imaging.make_gridding_convolution_function import gcf_tables
+    T, B, C, P = vis_d.shape
+    npad, cell = gp['image_size_padded'], gp['cell_size']
+    os_ = np.asarray(obs.oversampling)
+    band = (float(obs.freq.min()), float(obs.freq.max()))
+    lg = LearnedGCF.fit('casa_airy', obs.dish, obs.blockage, band, gp, os_, obs.max_support,
+                        n_freq=args.learned_freqs, steps=args.learned_steps, batch=65536)
+
+    def step_learned():
+        return lg.grid(vis_d, uvw_d, w_d, f_d, fidx_d, sl_d, npad, cell, layout='fft')
+
+    for _ in range(2):
+        gl, swl = step_learned()
+    stream = torch.cuda.current_stream()
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    torch.cuda.synchronize()
+    e0.record(stream)
+    for _ in range(args.steps):
+        gl, swl = step_learned()
+    e1.record(stream)
+    torch.cuda.synchronize()
+    ms_l = e0.elapsed_time(e1) / args.steps
+    # the tensor-core synthesis alone: every (channel, offset, tap) of the tables
+    S = int(lg.support_for(obs.freq).max()) | 1
+    n_eval = C * (int(os_[0]) + 1) * (int(os_[1]) + 1) * S * S
+    zz = torch.zeros((n_eval, 3), dtype=torch.float32, device='cuda')
+    _lib.mlp_forward(lg.params, zz[:1024], tensor_cores=True)
+    torch.cuda.synchronize()
+    e0.record(stream)
+    _lib.mlp_forward(lg.params, zz, tensor_cores=True)
+    e1.record(stream)
+    torch.cuda.synchronize()
+    ms_tc = e0.elapsed_time(e1)
+    flop = 2.0 * 3 * 4 * 64 * 64 * n_eval       # 4 layers, split-BF16 = 3 MMAs per product
+    del zz
+    # exact-frequency table path (one CF per channel)
+    ck_x, _, sup_x = gcf_tables('casa_airy', [obs.dish], [obs.blockage], np.array([[0, 0]]), obs.freq, gp, os_,
+                                obs.max_support, 0.025)
+    cfc = torch.arange(C, dtype=torch.int32, device='cuda')
+    zb = torch.zeros(B, dtype=torch.int32, device='cuda')
+    zp = torch.zeros(P, dtype=torch.int32, device='cuda')
+    gx, swx = _lib.grid_gcf(vis_d, uvw_d, w_d, f_d, fidx_d, zb, cfc, zp, ck_x, torch.as_tensor(sup_x.reshape(1, C, 1, 2),
+                            dtype=torch.int32, device='cuda'), sl_d, npad, cell, os_, layout='fft')
+    chans = sorted(set([0, C // 2, C - 1]))
+    i_tab, i_x, i_l = _dirty(g_tab, sw_tab, chans), _dirty(gx, swx, chans), _dirty(gl, swl, chans)
+    pk = np.abs(i_x).max()
+    rel = lambda a, b: float(np.abs(a - b).max() / pk)
+    return {
+        'train': {'n_samples': lg.info['n_samples'], 'n_freq': lg.info['n_freq'], 'steps': lg.info['steps'],
+                  'batch': lg.info['batch'], 'data_s': lg.info['data_s'], 'train_s': lg.info['train_s'],
+                  'final_loss': lg.info['final_loss'], 'kernels': 'ngg_mlp_train (own FP32 fwd/bwd/Adam)'},
+        'ms_learned_grid': ms_l, 'ms_table_grid': ms_tab, 'gcf_generation_s': t_gcf,
+        'speedup_grid_only': ms_tab / ms_l,
+        'speedup_incl_gcf_generation': (ms_tab + t_gcf * 1e3) / ms_l,
+        'tc_synthesis': {'evaluations': n_eval, 'ms': ms_tc, 'tflops': flop / (ms_tc * 1e-3) / 1e12,
+                         'naive_per_tap_evaluations': int(T * B * C * P) * S * S},
+        'image_err_learned_vs_table': rel(i_l, i_tab), 'image_err_learned_vs_exact_table': rel(i_l, i_x),
+        'image_err_table_vs_exact_table': rel(i_tab, i_x),
+        'images': f'dirty images (Re FFT^-1 / sum_weight) of channels {chans}, both pols, peak-normalised by the '
+                  f'exact-frequency table image',
+        'table_bytes': int(ck_x.numel() * 8), 'network_bytes': int(_lib.MLP_NPARAM * 4),
+    }
+
+
 def run_mosaic(args, rank, world, local, dist):
     """Mosaic aperture-projection imaging with the table GCF (one step =
     ngg_grid_gcf of the whole cube, inputs resident in HBM)."""
@@ -298,6 +384,10 @@ def run_mosaic(args, rank, world, local, dist):
                'note': 'make_image_with_gcf (flat_sky) on host numpy datasets: H2D of vis/weights/uvw/FIELD_ID, '
                        'gridding, cuFFT, normalisation, D2H of the float64 image; wall clock'}
 
+    learned = None
+    if not args.no_learned:
+        learned = learned_leg(args, obs, gcf, gp, vis_d, uvw_d, w_d, f_d, fidx_d, sl_d, g, sw, ms, t_gcf)
+
     cpu = None
     err = None
     if rank == 0 and not args.no_cpu:
@@ -338,7 +428,7 @@ def run_mosaic(args, rank, world, local, dist):
                        'gcf_generation_s': t_gcf, 'l2': 'inputs (0.7 GB) and grid (1.5 GB) exceed L2; no flush',
                        'parallelism': f'replica x{world}'},
             'roofline': roofline, 'cpu_baseline': cpu, 'e2e': e2e, 'err_vs_fp64': err, 'clocks': clk,
-            'gpu_launches': 6 * args.steps,
+            'gpu_launches': 6 * args.steps, 'learned_gcf': learned,
         }
         print(json.dumps(line), flush=True)
 

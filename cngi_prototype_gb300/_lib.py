@@ -52,6 +52,14 @@ class NggGcfArgs(ctypes.Structure):
                 ('conv_kernel', _vp), ('support', _vp), ('phase_slope', _vp), ('grid', _vp), ('sum_weight', _vp)]
 
 
+class NggMlpScale(ctypes.Structure):
+    _fields_ = [('x_scale', ctypes.c_double), ('y_scale', ctypes.c_double), ('f_center', ctypes.c_double),
+                ('f_scale', ctypes.c_double), ('out_scale', ctypes.c_double)]
+
+
+MLP_NPARAM = 16833
+MLP_NTRAINED = 16705
+
 # exported symbol -> (restype, argtypes)
 SIGNATURES = {
     'ngg_version': (ctypes.c_int, []),
@@ -78,6 +86,14 @@ SIGNATURES = {
                                             ctypes.POINTER(ctypes.c_int), ctypes.c_int,
                                             ctypes.POINTER(ctypes.c_int64), _vp]),
     'ngg_sqrt_abs': (ctypes.c_int, [_vp, _i64, _vp, _vp]),
+    'ngg_mlp_forward': (ctypes.c_int, [_vp, _vp, _i64, _vp, _vp]),
+    'ngg_mlp_forward_tc': (ctypes.c_int, [_vp, _vp, _i64, _vp, _vp]),
+    'ngg_mlp_loss_grad': (ctypes.c_int, [_vp, _vp, _vp, _i64, _vp, _vp, _vp]),
+    'ngg_mlp_adam': (ctypes.c_int, [_vp, _vp, _vp, _vp, ctypes.c_float, ctypes.c_float, ctypes.c_float,
+                                    ctypes.c_float, ctypes.c_int, _vp]),
+    'ngg_mlp_train': (ctypes.c_int, [_vp, _vp, _vp, _vp, _vp, _i64, _i64, ctypes.c_int, ctypes.c_int,
+                                     ctypes.c_float, ctypes.c_float, ctypes.c_uint64, _vp, _vp]),
+    'ngg_grid_gcf_learned': (ctypes.c_int, [ctypes.POINTER(NggGcfArgs), _vp, ctypes.POINTER(NggMlpScale), _vp]),
     'ngg_set_profiling': (None, [ctypes.c_int]),
     'ngg_last_phase_ms': (ctypes.c_int, [ctypes.POINTER(ctypes.c_double), ctypes.POINTER(ctypes.c_double)]),
     'ngg_release_cache': (None, []),
@@ -432,6 +448,100 @@ def sqrt_abs(x):
     out = torch.empty_like(x)
     _check(load().ngg_sqrt_abs(_ptr(x), int(x.numel()), _ptr(out), _stream()), 'ngg_sqrt_abs')
     return out
+
+
+def _params(params):
+    torch = _torch()
+    p = _dev(params, torch.float32, 'params')
+    if p.numel() != MLP_NPARAM:
+        raise NggError(f'params must hold {MLP_NPARAM} float32 values')
+    return p
+
+
+def mlp_forward(params, z, tensor_cores=False):
+    """Network output for z (n, 3) float32: FP32 CUDA cores, or the tcgen05 BF16 path."""
+    torch = _torch()
+    p = _params(params)
+    z_t = _dev(z, torch.float32, 'z')
+    n = int(z_t.shape[0])
+    y = torch.empty((n,), dtype=torch.float32, device='cuda')
+    f = load().ngg_mlp_forward_tc if tensor_cores else load().ngg_mlp_forward
+    _check(f(_ptr(p), _ptr(z_t), n, _ptr(y), _stream()), 'ngg_mlp_forward' + ('_tc' if tensor_cores else ''))
+    return y
+
+
+def mlp_loss_grad(params, z, target):
+    torch = _torch()
+    p = _params(params)
+    z_t = _dev(z, torch.float32, 'z')
+    t_t = _dev(target, torch.float32, 'target')
+    g = torch.empty((MLP_NPARAM,), dtype=torch.float32, device='cuda')
+    loss = torch.empty((1,), dtype=torch.float64, device='cuda')
+    _check(load().ngg_mlp_loss_grad(_ptr(p), _ptr(z_t), _ptr(t_t), int(z_t.shape[0]), _ptr(g), _ptr(loss), _stream()),
+           'ngg_mlp_loss_grad')
+    return float(loss.item()), g
+
+
+def mlp_adam(params, grad, m, v, step, lr, beta1=0.9, beta2=0.999, eps=1e-8):
+    """In-place Adam step on the CUDA tensors params / m / v."""
+    _check(load().ngg_mlp_adam(_ptr(params), _ptr(grad), _ptr(m), _ptr(v), float(lr), float(beta1), float(beta2),
+                               float(eps), int(step), _stream()), 'ngg_mlp_adam')
+
+
+def mlp_train(params, m, v, z, target, n_steps, step0=0, batch=65536, lr0=3e-3, lr1=3e-5, seed=0):
+    """n_steps Adam steps on random batches, in place; returns the per-step loss (CUDA float64)."""
+    torch = _torch()
+    z_t = _dev(z, torch.float32, 'z')
+    t_t = _dev(target, torch.float32, 'target')
+    hist = torch.empty((max(int(n_steps), 1),), dtype=torch.float64, device='cuda')
+    _check(load().ngg_mlp_train(_ptr(params), _ptr(m), _ptr(v), _ptr(z_t), _ptr(t_t), int(z_t.shape[0]), int(batch),
+                                int(n_steps), int(step0), float(lr0), float(lr1), ctypes.c_uint64(int(seed)),
+                                _ptr(hist), _stream()), 'ngg_mlp_train')
+    return hist[:int(n_steps)]
+
+
+def grid_gcf_learned(vis, uvw, weight, freq, field_index, support, phase_slope, params, scale, conv_size, n_uv,
+                     delta_lm, oversampling, mode='data', chan_mode='cube', layout='natural'):
+    """Mosaic gridder with per-channel GCF tables synthesised by the network.
+    support int32 (C, 2) per channel; scale: dict of NggMlpScale fields."""
+    torch = _torch()
+    uvw_t = _dev(uvw, torch.float64, 'uvw')
+    w_t = _dev(weight, torch.float32, 'weight')
+    f_t = _dev(freq, torch.float64, 'freq')
+    fidx_t = _dev(field_index, torch.int32, 'field_index')
+    sup_t = _dev(support, torch.int32, 'support')
+    slope_t = _dev(phase_slope, torch.float64, 'phase_slope')
+    p = _params(params)
+    T, B, C, P = w_t.shape
+    if tuple(sup_t.shape) != (C, 2):
+        raise NggError('support must be (n_chan, 2)')
+    v_t = _dev(vis, torch.complex64, 'vis') if mode == 'data' else None
+    n_img = 1 if chan_mode == 'continuum' else C
+    grid = torch.empty((n_img, P, int(n_uv[0]), int(n_uv[1])), dtype=torch.complex64, device='cuda')
+    sw = torch.empty((n_img, P), dtype=torch.float64, device='cuda')
+    a = NggGcfArgs()
+    a.mode = MODES[mode]
+    a.chan_mode = CHAN_MODES[chan_mode]
+    a.layout = LAYOUTS[layout]
+    a.oversampling[0], a.oversampling[1] = int(oversampling[0]), int(oversampling[1])
+    a.n_field = int(slope_t.shape[0])
+    a.n_time, a.n_baseline, a.n_chan, a.n_pol = T, B, C, P
+    a.n_u, a.n_v = int(n_uv[0]), int(n_uv[1])
+    a.delta_lm[0], a.delta_lm[1] = float(delta_lm[0]), float(delta_lm[1])
+    a.n_cf_baseline, a.n_cf_chan, a.n_cf_pol = 1, C, 1
+    a.conv_size[0], a.conv_size[1] = int(conv_size[0]), int(conv_size[1])
+    a.vis = _ptr(v_t).value
+    a.uvw = _ptr(uvw_t).value
+    a.weight = _ptr(w_t).value
+    a.freq = _ptr(f_t).value
+    a.field_index = _ptr(fidx_t).value
+    a.support = _ptr(sup_t).value
+    a.phase_slope = _ptr(slope_t).value
+    a.grid = _ptr(grid).value
+    a.sum_weight = _ptr(sw).value
+    sc = NggMlpScale(**{k: float(scale[k]) for k in ('x_scale', 'y_scale', 'f_center', 'f_scale', 'out_scale')})
+    _check(load().ngg_grid_gcf_learned(ctypes.byref(a), _ptr(p), ctypes.byref(sc), _stream()), 'ngg_grid_gcf_learned')
+    return grid, sw
 
 
 def set_profiling(enable=True):

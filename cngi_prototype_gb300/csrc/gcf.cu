@@ -30,6 +30,7 @@
 
 #include "ngg_internal.cuh"
 #include "gcf_grid.cuh"
+#include "mlp.cuh"
 
 namespace ngg {
 namespace {
@@ -116,21 +117,18 @@ __global__ void k_cell_phase(const double *slope, int nf, int64_t nu, int64_t nv
     hy[f * (os1 + 1) + x] = make_float2((float)c, (float)s);
 }
 
-// per-field phase tables: ex[f][x] = exp(i (x - R0/2) px_f), ey likewise, in
-// FP32 for the taps and FP64 for the tap sums
-__global__ void k_phase_tabs(const double *slope, int nf, int64_t R0, int64_t R1, float2 *ex, float2 *ey,
-                             double2 *ex64, double2 *ey64) {
+// per-field FP64 phase tables for the tap sums: ex[f][x] = exp(i (x - R0/2) px_f),
+// ey likewise
+__global__ void k_phase_tabs(const double *slope, int nf, int64_t R0, int64_t R1, double2 *ex64, double2 *ey64) {
     const int64_t id = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
     if (id >= (int64_t)nf * (R0 + R1)) return;
     const int64_t f = id / (R0 + R1), x = id % (R0 + R1);
     double s, c;
     if (x < R0) {
         sincos((double)(x - R0 / 2) * slope[f * 2 + 0], &s, &c);
-        ex[f * R0 + x] = make_float2((float)c, (float)s);
         ex64[f * R0 + x] = make_double2(c, s);
     } else {
         sincos((double)(x - R0 - R1 / 2) * slope[f * 2 + 1], &s, &c);
-        ey[f * R1 + (x - R0)] = make_float2((float)c, (float)s);
         ey64[f * R1 + (x - R0)] = make_double2(c, s);
     }
 }
@@ -325,7 +323,41 @@ __global__ void k_sqrt_abs(const double *w, int64_t n, double *pb) {
     if (id < n) pb[id] = sqrt(fabs(w[id]));
 }
 
-int check_gcf(const NggGcfArgs *a) {
+// the same tap sums from the reorganised FP32 table ckt (learned path)
+__global__ void k_norms_tab(const float *ckt, const double2 *ex64, const double2 *ey64, int nf, int64_t ncf,
+                            int64_t R0, int64_t R1, int os0, int os1, int S, double2 *nrm) {
+    const int64_t no = (int64_t)(os0 + 1) * (os1 + 1);
+    const int64_t id = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (id >= nf * ncf * no) return;
+    const int64_t f = id / (ncf * no), cf = (id / no) % ncf, o = id % no;
+    const int oui = (int)(o / (os1 + 1)), ovi = (int)(o % (os1 + 1));
+    const int sc = S / 2;
+    const float *blk = ckt + ((cf * (os0 + 1) + oui) * (os1 + 1) + ovi) * (2 * S) * SP;
+    double re = 0.0, im = 0.0;
+    for (int dv = 0; dv < S; ++dv) {
+        const int64_t y = (int64_t)os1 * (dv - sc) + ovi - os1 / 2 + R1 / 2;
+        const double2 e = ey64[f * R1 + y];
+        double rr = 0.0, ri = 0.0;
+        for (int du = 0; du < S; ++du) {
+            const double k = blk[dv * SP + du];
+            if (k == 0.0) continue;
+            const int64_t x = (int64_t)os0 * (du - sc) + oui - os0 / 2 + R0 / 2;
+            const double2 q = ex64[f * R0 + x];
+            rr += k * q.x;
+            ri += k * q.y;
+        }
+        re += rr * e.x - ri * e.y;
+        im += rr * e.y + ri * e.x;
+    }
+    nrm[id] = make_double2(re, im);
+}
+
+__global__ void k_iota(int32_t *p, int64_t n) {
+    const int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (i < n) p[i] = (int32_t)i;
+}
+
+int check_gcf(const NggGcfArgs *a, bool learned = false) {
     if (!a) return fail(NGG_ERR_INVALID, "args is NULL");
     if (a->chan_mode != NGG_CHAN_CUBE && a->chan_mode != NGG_CHAN_CONTINUUM) return fail(NGG_ERR_INVALID, "chan_mode");
     if (a->layout != NGG_LAYOUT_NATURAL && a->layout != NGG_LAYOUT_FFT) return fail(NGG_ERR_INVALID, "layout");
@@ -336,28 +368,24 @@ int check_gcf(const NggGcfArgs *a) {
         return fail(NGG_ERR_UNSUPPORTED, "oversampling out of [1,1000]");
     if (a->n_cf_baseline < 1 || a->n_cf_chan < 1 || a->n_cf_pol < 1 || a->conv_size[0] < 1 || a->conv_size[1] < 1)
         return fail(NGG_ERR_INVALID, "GCF table dims");
-    if (!a->grid || !a->sum_weight || !a->conv_kernel || !a->support || !a->phase_slope || !a->cf_baseline_map ||
-        !a->cf_chan_map || !a->cf_pol_map)
+    if (!a->grid || !a->sum_weight || !a->support || !a->phase_slope) return fail(NGG_ERR_INVALID, "NULL pointer");
+    if (!learned && (!a->conv_kernel || !a->cf_baseline_map || !a->cf_chan_map || !a->cf_pol_map))
         return fail(NGG_ERR_INVALID, "NULL pointer");
     return NGG_OK;
 }
 
-struct GScratch {
-    std::vector<void *> v;
-    cudaStream_t s;
-    explicit GScratch(cudaStream_t st) : s(st) {}
-    int get(void **p, size_t n) {
-        int rc = scratch_alloc(p, n, s);
-        if (rc == NGG_OK) v.push_back(*p);
-        return rc;
-    }
-    ~GScratch() {
-        for (void *p : v) scratch_free(p, s);
-    }
-};
+
 
 // shared set-up of both gridders; returns the maximum support via *maxsup
-int gcf_setup(const NggGcfArgs *a, cudaStream_t s, GScratch &sc, GArgs &g, int *S_out) {
+struct Learned {
+    const float *params;
+    const NggMlpScale *scale;
+};
+
+// learned: the per-channel tables come from the network (conv_kernel and the
+// CF maps are not read)
+int gcf_setup(const NggGcfArgs *a, cudaStream_t s, ScratchList &sc, GArgs &g, int *S_out,
+              const Learned *learned = nullptr) {
     const int64_t T = a->n_time, B = a->n_baseline, C = a->n_chan, P = a->n_pol;
     const int64_t ncf = a->n_cf_baseline * a->n_cf_chan * a->n_cf_pol;
     // supports (host copy: small)
@@ -382,8 +410,8 @@ int gcf_setup(const NggGcfArgs *a, cudaStream_t s, GScratch &sc, GArgs &g, int *
     float4 *uvs = nullptr;
     float *ckt = nullptr;
     float2 *gx = nullptr, *gy = nullptr, *hx = nullptr, *hy = nullptr;
-    float2 *ex = nullptr, *ey = nullptr;
     double2 *ex64 = nullptr, *ey64 = nullptr;
+    int32_t *maps = nullptr;
     double2 *nrm = nullptr;
     if ((rc = sc.get((void **)&chan, sizeof(GChan) * (C > 0 ? C : 1))) != NGG_OK) return rc;
     if ((rc = sc.get((void **)&uvs, sizeof(float4) * (T * B > 0 ? T * B : 1))) != NGG_OK) return rc;
@@ -394,25 +422,37 @@ int gcf_setup(const NggGcfArgs *a, cudaStream_t s, GScratch &sc, GArgs &g, int *
     if ((rc = sc.get((void **)&gy, sizeof(float2) * nf * a->n_v)) != NGG_OK) return rc;
     if ((rc = sc.get((void **)&hx, sizeof(float2) * nf * (a->oversampling[0] + 1))) != NGG_OK) return rc;
     if ((rc = sc.get((void **)&hy, sizeof(float2) * nf * (a->oversampling[1] + 1))) != NGG_OK) return rc;
-    if ((rc = sc.get((void **)&ex, sizeof(float2) * a->n_field * a->conv_size[0])) != NGG_OK) return rc;
-    if ((rc = sc.get((void **)&ey, sizeof(float2) * a->n_field * a->conv_size[1])) != NGG_OK) return rc;
     if ((rc = sc.get((void **)&ex64, sizeof(double2) * a->n_field * a->conv_size[0])) != NGG_OK) return rc;
     if ((rc = sc.get((void **)&ey64, sizeof(double2) * a->n_field * a->conv_size[1])) != NGG_OK) return rc;
     const int64_t nn = a->n_field * ncf * (a->oversampling[0] + 1) * (a->oversampling[1] + 1);
     if ((rc = sc.get((void **)&nrm, sizeof(double2) * nn)) != NGG_OK) return rc;
     if (C > 0) k_gchan<<<(unsigned)((C + 127) / 128), 128, 0, s>>>(a->freq, (int)C, a->delta_lm[0], a->delta_lm[1], a->n_u, a->n_v, chan);
     if (T * B > 0) k_gsplit<<<(unsigned)((T * B + 255) / 256), 256, 0, s>>>(a->uvw, T * B, uvs);
-    k_reorg<<<(unsigned)((nck + 255) / 256), 256, 0, s>>>(a->conv_kernel, ncf, a->conv_size[0], a->conv_size[1],
-                                                         a->oversampling[0], a->oversampling[1], a->support, S, ckt);
+    if (learned) {
+        if ((rc = sc.get((void **)&maps, sizeof(int32_t) * (B + C + P + 1))) != NGG_OK) return rc;
+        NGG_CUDA(cudaMemsetAsync(maps, 0, sizeof(int32_t) * (B + C + P + 1), s));
+        if (C > 0) k_iota<<<(unsigned)((C + 255) / 256), 256, 0, s>>>(maps + B, C);
+        if ((rc = mlp_synth_table(learned->params, learned->scale, a->freq, C, a->oversampling[0], a->oversampling[1],
+                                  S, a->support, ckt, s)) != NGG_OK)
+            return rc;
+    } else {
+        k_reorg<<<(unsigned)((nck + 255) / 256), 256, 0, s>>>(a->conv_kernel, ncf, a->conv_size[0], a->conv_size[1],
+                                                             a->oversampling[0], a->oversampling[1], a->support, S, ckt);
+    }
     const int64_t ncp = nf * (a->n_u + a->n_v + a->oversampling[0] + 1 + a->oversampling[1] + 1);
     k_cell_phase<<<(unsigned)((ncp + 255) / 256), 256, 0, s>>>(a->phase_slope, a->n_field, a->n_u, a->n_v,
                                                               a->oversampling[0], a->oversampling[1], gx, gy, hx, hy);
     const int64_t npt = (int64_t)a->n_field * (a->conv_size[0] + a->conv_size[1]);
     k_phase_tabs<<<(unsigned)((npt + 255) / 256), 256, 0, s>>>(a->phase_slope, a->n_field, a->conv_size[0],
-                                                              a->conv_size[1], ex, ey, ex64, ey64);
-    k_norms<<<(unsigned)((nn + 127) / 128), 128, 0, s>>>(a->conv_kernel, a->support, ex64, ey64, a->n_field, ncf,
-                                                        a->conv_size[0], a->conv_size[1], a->oversampling[0],
-                                                        a->oversampling[1], 0, nrm);
+                                                              a->conv_size[1], ex64, ey64);
+    if (learned)
+        k_norms_tab<<<(unsigned)((nn + 127) / 128), 128, 0, s>>>(ckt, ex64, ey64, a->n_field, ncf, a->conv_size[0],
+                                                                a->conv_size[1], a->oversampling[0],
+                                                                a->oversampling[1], S, nrm);
+    else
+        k_norms<<<(unsigned)((nn + 127) / 128), 128, 0, s>>>(a->conv_kernel, a->support, ex64, ey64, a->n_field, ncf,
+                                                            a->conv_size[0], a->conv_size[1], a->oversampling[0],
+                                                            a->oversampling[1], 0, nrm);
     NGG_CHECK_LAUNCH("gcf set-up kernels");
     g.vis = (const float2 *)a->vis;
     g.weight = a->weight;
@@ -420,13 +460,11 @@ int gcf_setup(const NggGcfArgs *a, cudaStream_t s, GScratch &sc, GArgs &g, int *
     g.uvs = uvs;
     g.chan = chan;
     g.field_index = a->field_index;
-    g.cfb_map = a->cf_baseline_map;
-    g.cfc_map = a->cf_chan_map;
-    g.cfp_map = a->cf_pol_map;
+    g.cfb_map = learned ? maps : a->cf_baseline_map;
+    g.cfc_map = learned ? maps + B : a->cf_chan_map;
+    g.cfp_map = learned ? maps + B + C : a->cf_pol_map;
     g.ckt = ckt;
     g.gx = gx; g.gy = gy; g.hx = hx; g.hy = hy;
-    g.ex = ex;
-    g.ey = ey;
     g.ex64 = ex64;
     g.ey64 = ey64;
     g.nrm = nrm;
@@ -463,10 +501,37 @@ extern "C" int ngg_grid_gcf(const NggGcfArgs *a, void *stream) {
     if (a->n_time * a->n_baseline * a->n_chan == 0) return NGG_OK;
     if (!a->uvw || !a->weight || !a->freq || !a->field_index || (a->mode == NGG_MODE_DATA && !a->vis))
         return fail(NGG_ERR_INVALID, "NULL input");
-    GScratch sc(s);
+    ScratchList sc(s);
     GArgs g;
     int S = 0;
     if ((rc = gcf_setup(a, s, sc, g, &S)) != NGG_OK) return rc;
+    const int64_t items = a->n_chan * a->n_baseline * g.nk * a->n_pol;
+    const unsigned blocks = (unsigned)((items + 3) / 4);
+    const bool data = a->mode == NGG_MODE_DATA;
+    if (S <= 15) return launch_grid_gcf_lo(g, data, blocks, s);
+    return S <= 23 ? launch_grid_gcf_mid(g, data, blocks, s) : launch_grid_gcf_hi(g, data, blocks, s);
+}
+
+extern "C" int ngg_grid_gcf_learned(const NggGcfArgs *a, const float *params, const NggMlpScale *scale, void *stream) {
+    clear_error();
+    int rc = check_gcf(a, true);
+    if (rc != NGG_OK) return rc;
+    if (!params || !scale) return fail(NGG_ERR_INVALID, "params / scale is NULL");
+    if (a->n_cf_baseline != 1 || a->n_cf_pol != 1 || a->n_cf_chan != a->n_chan)
+        return fail(NGG_ERR_INVALID, "learned GCF: one table per channel (n_cf_chan = n_chan, n_cf_baseline = n_cf_pol = 1)");
+    cudaStream_t s = (cudaStream_t)stream;
+    const int64_t n_img = a->chan_mode == NGG_CHAN_CONTINUUM ? 1 : a->n_chan;
+    if (n_img == 0) return NGG_OK;
+    NGG_CUDA(cudaMemsetAsync(a->grid, 0, sizeof(float2) * n_img * a->n_pol * a->n_u * a->n_v, s));
+    NGG_CUDA(cudaMemsetAsync(a->sum_weight, 0, sizeof(double) * n_img * a->n_pol, s));
+    if (a->n_time * a->n_baseline * a->n_chan == 0) return NGG_OK;
+    if (!a->uvw || !a->weight || !a->freq || !a->field_index || (a->mode == NGG_MODE_DATA && !a->vis))
+        return fail(NGG_ERR_INVALID, "NULL input");
+    ScratchList sc(s);
+    GArgs g;
+    int S = 0;
+    Learned L{params, scale};
+    if ((rc = gcf_setup(a, s, sc, g, &S, &L)) != NGG_OK) return rc;
     const int64_t items = a->n_chan * a->n_baseline * g.nk * a->n_pol;
     const unsigned blocks = (unsigned)((items + 3) / 4);
     const bool data = a->mode == NGG_MODE_DATA;
@@ -485,7 +550,7 @@ extern "C" int ngg_grid_gcf_weight(const NggGcfArgs *a, void *stream) {
     NGG_CUDA(cudaMemsetAsync(a->sum_weight, 0, sizeof(double) * n_img * a->n_pol, s));
     if (a->n_time * a->n_baseline * a->n_chan == 0) return NGG_OK;
     if (!a->uvw || !a->weight || !a->freq || !a->field_index) return fail(NGG_ERR_INVALID, "NULL input");
-    GScratch sc(s);
+    ScratchList sc(s);
     GArgs g;
     int S = 0;
     if ((rc = gcf_setup(a, s, sc, g, &S)) != NGG_OK) return rc;
@@ -523,7 +588,7 @@ extern "C" int ngg_gcf_kernels(int casa_model, int64_t nt, const double *dish, c
         for (auto x : hp)
             if (x < 0 || x >= nt) return fail(NGG_ERR_INVALID, "antenna-type pair index out of range");
     }
-    GScratch sc(s);
+    ScratchList sc(s);
     double *pat = nullptr;
     double2 *work = nullptr;
     int rc;
@@ -576,7 +641,7 @@ extern "C" int ngg_mosaic_normalize(double *image, int64_t n_l, int64_t n_m, int
     NGG_CHECK_LAUNCH("k_mnorm");
     if (centre) {
         // the centre pixels of every plane are copied out first (they are divided too)
-        GScratch sc(s);
+        ScratchList sc(s);
         double *cval = nullptr;
         int rc;
         if ((rc = sc.get((void **)&cval, sizeof(double) * n_planes)) != NGG_OK) return rc;

@@ -24,7 +24,6 @@ struct GArgs {
     const int32_t *field_index, *cfb_map, *cfc_map, *cfp_map;
     const float *ckt;
     const float2 *gx, *gy, *hx, *hy;
-    const float2 *ex, *ey;
     const double2 *ex64, *ey64;
     const double2 *nrm;
     float2 *grid;

@@ -35,6 +35,25 @@ void scratch_free(void *p, cudaStream_t s);
 
 int num_sms();
 
+// Scratch blocks released (stream-ordered) when the list goes out of scope.
+struct ScratchList {
+    void *p[32];
+    int n = 0;
+    cudaStream_t s;
+    explicit ScratchList(cudaStream_t st) : s(st) {}
+    int get(void **out, size_t bytes) {
+        if (n == 32) return fail(NGG_ERR_INVALID, "too many scratch blocks");
+        int rc = scratch_alloc(out, bytes, s);
+        if (rc == NGG_OK) p[n++] = *out;
+        return rc;
+    }
+    ~ScratchList() {
+        for (int i = 0; i < n; ++i) scratch_free(p[i], s);
+    }
+    ScratchList(const ScratchList &) = delete;
+    ScratchList &operator=(const ScratchList &) = delete;
+};
+
 // ---- exact reproduction of the reference's FP64 index arithmetic ---------
 //
 // The reference computes, in FP64 with one rounding per operation

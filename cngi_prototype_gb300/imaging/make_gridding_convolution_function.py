@@ -104,6 +104,50 @@ def _phase_gradient(slopes, conv_size):
     return torch.polar(torch.ones_like(ph), ph)
 
 
+def gcf_tables(function, dish, blockage, pairs, pb_freq, grid_parms, oversampling, max_support, support_cut_level,
+               freq_chunk=8):
+    """CONV_KERNEL and WEIGHT_CONV_KERNEL (n_pair, n_freq, 1, R0, R1) float64 CUDA
+    tensors and SUPPORT (n_pair, n_freq, 1, 2) (make_gridding_convolution_function.py:
+    164-274 and resize_and_calc_support, :360-390): patterns and FFTs on the GPU
+    (ngg_gcf_kernels) in chunks of PB frequencies; the support walk on the
+    kernels' centre row and column; crop to (max_support + 1) * os and division
+    by the sum over the (support + 1) * os window / (os0 * os1) on the device."""
+    import torch
+    os_ = np.asarray(oversampling)
+    max_sup = np.asarray(max_support)
+    rs = (max_sup + 1) * os_
+    npad = np.asarray(grid_parms['image_size_padded'])
+    cell = np.asarray(grid_parms['cell_size']) * os_
+    pb_freq = np.asarray(pb_freq, dtype=np.float64)
+    n_pair, n_freq = len(pairs), len(pb_freq)
+    c0, c1 = int(npad[0] // 2), int(npad[1] // 2)
+    st = npad // 2 - rs // 2
+    support = np.zeros((n_pair, n_freq, 1, 2), dtype=int)
+    ck = torch.empty((n_pair, n_freq, 1, int(rs[0]), int(rs[1])), dtype=torch.float64, device='cuda')
+    wk = torch.empty_like(ck)
+    for f0 in range(0, n_freq, freq_chunk):
+        fr = pb_freq[f0:f0 + freq_chunk]
+        ck_full, wk_full = _lib.gcf_kernels(function, dish, blockage, pairs, fr, npad, cell, npad // 2)
+        awk = wk_full.abs()
+        amax = awk.amax(dim=(2, 3)).cpu().numpy()
+        amin = awk.amin(dim=(2, 3)).cpu().numpy()
+        rows = wk_full[:, :, :, c1].cpu().numpy()
+        cols = wk_full[:, :, c0, :].cpu().numpy()
+        for q in range(n_pair):
+            for j in range(len(fr)):
+                f = f0 + j
+                support[q, f, 0] = calc_conv_size(rows[q, j], cols[q, j], amin[q, j], amax[q, j], npad,
+                                                  support_cut_level, os_, max_sup)
+                es = (support[q, f, 0] + 1) * os_
+                e0 = rs // 2 - es // 2
+                for src, dst in ((ck_full, ck), (wk_full, wk)):
+                    crop = src[q, j, st[0]:st[0] + rs[0], st[1]:st[1] + rs[1]]
+                    nf = crop[e0[0]:e0[0] + es[0], e0[1]:e0[1] + es[1]].sum() / float(os_[0] * os_[1])
+                    dst[q, f, 0] = crop / nf
+        del ck_full, wk_full, awk
+    return ck, wk, support
+
+
 def _baseline_ant(vis):
     a1 = np.asarray(vis['ANTENNA1'].values)
     a2 = np.asarray(vis['ANTENNA2'].values)
@@ -158,32 +202,8 @@ def make_gridding_convolution_function(mxds, gcf_parms, grid_parms, sel_parms):
     cf_chan_map, pb_freq = create_cf_chan_map(_gcf['freq_chan'], _gcf['chan_tolerance_factor'])
     cf_pol_map = np.zeros(len(_gcf['pol']), dtype=int)
 
-    # baseline patterns and their FFTs: (pair, pb_freq, n0, n1) float64 on the device
-    cell = np.asarray(_gp['cell_size']) * os_
-    ck_full, wk_full = _lib.gcf_kernels(_gcf['function'], _gcf['list_dish_diameters'],
-                                        _gcf['list_blockage_diameters'], pairs, pb_freq, npad, cell, npad // 2)
-    n_pair, n_freq = ck_full.shape[:2]
-    c0, c1 = int(npad[0] // 2), int(npad[1] // 2)
-    awk = wk_full.abs()
-    amax = awk.amax(dim=(2, 3)).cpu().numpy()
-    amin = awk.amin(dim=(2, 3)).cpu().numpy()
-    rows = wk_full[:, :, :, c1].cpu().numpy()
-    cols = wk_full[:, :, c0, :].cpu().numpy()
-    support = np.zeros((n_pair, n_freq, 1, 2), dtype=int)
-    st = npad // 2 - rs // 2
-    ck = torch.empty((n_pair, n_freq, 1, int(rs[0]), int(rs[1])), dtype=torch.float64, device='cuda')
-    wk = torch.empty_like(ck)
-    for q in range(n_pair):
-        for f in range(n_freq):
-            support[q, f, 0] = calc_conv_size(rows[q, f], cols[q, f], amin[q, f], amax[q, f], npad,
-                                              _gcf['support_cut_level'], os_, max_sup)
-            es = (support[q, f, 0] + 1) * os_
-            e0 = rs // 2 - es // 2
-            for src, dst in ((ck_full, ck), (wk_full, wk)):
-                crop = src[q, f, st[0]:st[0] + rs[0], st[1]:st[1] + rs[1]]
-                nf = crop[e0[0]:e0[0] + es[0], e0[1]:e0[1] + es[1]].sum() / float(os_[0] * os_[1])
-                dst[q, f, 0] = crop / nf
-    del ck_full, wk_full, awk
+    ck, wk, support = gcf_tables(_gcf['function'], _gcf['list_dish_diameters'], _gcf['list_blockage_diameters'],
+                                 pairs, pb_freq, _gp, os_, max_sup, _gcf['support_cut_level'])
 
     slopes = _phase_slopes(_gcf['field_phase_dir'], _gcf['phase_center'], _gp, os_)
     pg = _phase_gradient(slopes, rs)

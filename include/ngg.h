@@ -294,6 +294,60 @@ int ngg_mosaic_normalize(double *image, int64_t n_l, int64_t n_m, int64_t n_plan
 /* out[i] = sqrt(|x[i]|): the mosaic PB from WEIGHT_PB (make_mosaic_pb.py:150). */
 int ngg_sqrt_abs(const double *x, int64_t n, double *out, void *stream);
 
+/* ---- learned GCF: coordinate MLP ------------------------------------------
+ * No counterpart in the reference (it has no learned component). A small
+ * network stands in for the CONV_KERNEL table of
+ * make_gridding_convolution_function (make_gridding_convolution_function.py:
+ * 164-311): inputs z = (x, y, f) scaled to about [-1, 1] (table offsets
+ * from the centre and frequency), c = (x, y, r = |(x, y)|, f), Fourier
+ * features [sin(2 pi B c), cos(2 pi B c)] (B: 32 x 4, fixed), four SiLU
+ * layers of width 64, one linear output. params: float32 vector of
+ * NGG_MLP_NPARAM values laid out W1[64][64] b1[64] W2 b2 W3 b3 W4 b4 Wo[64]
+ * bo B[32][4]; the first NGG_MLP_NTRAINED are trained. All pointers are
+ * device pointers. z float32 (n, 3); y, target float32 (n).
+ *
+ * ngg_mlp_forward: y = net(z), FP32 on CUDA cores (the training precision).
+ * ngg_mlp_forward_tc: the same network with the four 64x64 layers on the
+ *   tcgen05 tensor cores (BF16 operands, FP32 accumulation in tensor memory);
+ *   features and the output layer in FP32.
+ * ngg_mlp_loss_grad: loss = mean((y - target)^2) (float64, device) and its
+ *   gradient w.r.t. params (float32, NGG_MLP_NPARAM; zero for B).
+ * ngg_mlp_adam: one bias-corrected Adam step (step >= 1) on the trained
+ *   parameters; m, v float32 (NGG_MLP_NTRAINED).
+ * ngg_mlp_train: n_steps Adam steps on random batches (batch rows drawn by a
+ *   counter-based hash of (seed, step)) of the n_samples (z, target) pairs,
+ *   learning rate cosine-decayed from lr0 to lr1; steps are numbered from
+ *   step0 + 1; the loss of each step goes to loss_history (device float64,
+ *   n_steps) when it is not NULL. */
+typedef struct NggMlpScale {
+    double x_scale, y_scale;    /* z_x = x * x_scale, z_y = y * y_scale (x, y table offsets) */
+    double f_center, f_scale;   /* z_f = (f - f_center) * f_scale (Hz)                       */
+    double out_scale;           /* table value = net output * out_scale                      */
+} NggMlpScale;
+
+#define NGG_MLP_NPARAM 16833
+#define NGG_MLP_NTRAINED 16705
+int ngg_mlp_forward(const float *params, const float *z, int64_t n, float *y, void *stream);
+int ngg_mlp_forward_tc(const float *params, const float *z, int64_t n, float *y, void *stream);
+int ngg_mlp_loss_grad(const float *params, const float *z, const float *target, int64_t n, float *grad,
+                      double *loss, void *stream);
+int ngg_mlp_adam(float *params, const float *grad, float *m, float *v, float lr, float beta1, float beta2,
+                 float eps, int step, void *stream);
+int ngg_mlp_train(float *params, float *m, float *v, const float *z, const float *target, int64_t n_samples,
+                  int64_t batch, int n_steps, int step0, float lr0, float lr1, uint64_t seed,
+                  double *loss_history, void *stream);
+
+/* Mosaic gridding with the learned GCF in place of the table (the table path,
+ * ngg_grid_gcf, stays the fallback and the judge of its error). Same
+ * arguments as ngg_grid_gcf except: conv_kernel is not read; the GCF of
+ * channel c is the network evaluated at freq[c] (one table per channel, so
+ * n_cf_baseline = n_cf_pol = 1 and n_cf_chan = n_chan are required and the
+ * CF maps are not read); support (n_chan, 2) int32 gives each channel's
+ * support; conv_size = (max support + 1) * oversampling. The per-channel
+ * tables are synthesised on the tensor cores (ngg_mlp_forward_tc's kernel)
+ * for every tap and oversampling offset the gridder reads. */
+int ngg_grid_gcf_learned(const NggGcfArgs *args, const float *params, const NggMlpScale *scale, void *stream);
+
 /* Profiling: when enabled, ngg_grid_ps records CUDA events on its stream
  * around its binning phase and its tile-accumulation kernels. ngg_last_phase_ms
  * waits for the last call's events and returns the two durations (ms). */

@@ -323,7 +323,8 @@ __global__ void k_sqrt_abs(const double *w, int64_t n, double *pb) {
     if (id < n) pb[id] = sqrt(fabs(w[id]));
 }
 
-// the same tap sums from the reorganised FP32 table ckt (learned path)
+// the same tap sums from the reorganised FP32 table ckt (learned path): FP32
+// sums along a row, FP64 across rows (the table itself is a fit to ~1e-3)
 __global__ void k_norms_tab(const float *ckt, const double2 *ex64, const double2 *ey64, int nf, int64_t ncf,
                             int64_t R0, int64_t R1, int os0, int os1, int S, double2 *nrm) {
     const int64_t no = (int64_t)(os0 + 1) * (os1 + 1);
@@ -333,21 +334,20 @@ __global__ void k_norms_tab(const float *ckt, const double2 *ex64, const double2
     const int oui = (int)(o / (os1 + 1)), ovi = (int)(o % (os1 + 1));
     const int sc = S / 2;
     const float *blk = ckt + ((cf * (os0 + 1) + oui) * (os1 + 1) + ovi) * (2 * S) * SP;
+    const double2 *exf = ex64 + f * R0 + (oui - os0 / 2 + R0 / 2 - (int64_t)os0 * sc);
     double re = 0.0, im = 0.0;
     for (int dv = 0; dv < S; ++dv) {
         const int64_t y = (int64_t)os1 * (dv - sc) + ovi - os1 / 2 + R1 / 2;
         const double2 e = ey64[f * R1 + y];
-        double rr = 0.0, ri = 0.0;
+        float rr = 0.f, ri = 0.f;
         for (int du = 0; du < S; ++du) {
-            const double k = blk[dv * SP + du];
-            if (k == 0.0) continue;
-            const int64_t x = (int64_t)os0 * (du - sc) + oui - os0 / 2 + R0 / 2;
-            const double2 q = ex64[f * R0 + x];
-            rr += k * q.x;
-            ri += k * q.y;
+            const float k = blk[dv * SP + du];
+            const double2 q = exf[(int64_t)os0 * du];
+            rr = fmaf(k, (float)q.x, rr);
+            ri = fmaf(k, (float)q.y, ri);
         }
-        re += rr * e.x - ri * e.y;
-        im += rr * e.y + ri * e.x;
+        re += (double)rr * e.x - (double)ri * e.y;
+        im += (double)rr * e.y + (double)ri * e.x;
     }
     nrm[id] = make_double2(re, im);
 }

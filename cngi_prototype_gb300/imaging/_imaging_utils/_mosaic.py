@@ -47,7 +47,9 @@ def gcf_planes(kind, vis, uvw, imaging_weight, field, freq, gcf_xds, grid_parms)
     """Mosaic image planes before normalisation.
 
     kind: 'data' (make_image_with_gcf), 'psf' (make_psf_with_gcf) or
-    'weight' (make_mosaic_pb). Returns (image (l, m, Cimg, P) float64 CUDA
+    'weight' (make_mosaic_pb). When gcf_xds.attrs['learned_gcf'] holds a
+    LearnedGCF, the data / PSF grids use its per-channel tables (the weight
+    grid keeps WEIGHT_CONV_KERNEL). Returns (image (l, m, Cimg, P) float64 CUDA
     tensor = Re(FFT^-1 grid) * Nu*Nv / sum_weight, sum_weight (Cimg, P)
     float64 numpy).
     """
@@ -77,8 +79,16 @@ def gcf_planes(kind, vis, uvw, imaging_weight, field, freq, gcf_xds, grid_parms)
     for c0, c1 in chan_chunks(C, P, npad, chan_mode, GRID_BUDGET_BYTES):
         wv = _slice_chan(w, c0, c1) if (c0, c1) != (0, C) else w
         common = (uvw_d, wv, freq[c0:c1], fidx, cfb, cfc[c0:c1], cfp, ck_d, sup_d, slope_d)
+        learned = gcf_xds.attrs.get('learned_gcf') if hasattr(gcf_xds, 'attrs') else None
         if kind == 'weight':
             g, sw = _lib.grid_gcf_weight(*common, npad, cell, os_, chan_mode=chan_mode, layout='fft')
+        elif learned is not None:
+            vv = None
+            if kind == 'data':
+                v = _arr(vis)
+                vv = _slice_chan(v, c0, c1) if (c0, c1) != (0, C) else v
+            g, sw = learned.grid(vv, uvw_d, wv, freq[c0:c1], fidx, slope_d, npad, cell, mode=kind,
+                                 chan_mode=chan_mode, layout='fft')
         else:
             vv = None
             if kind == 'data':

@@ -132,3 +132,25 @@ def test_c_aperture_oracle_matches_reference(gold, tag):
                               gp['image_size_padded'], gp['cell_size'], d['oversampling'], 'continuum',
                               do_psf=kind == 'psf', weight_grid=kind == 'weight')
     assert np.array_equal(gc, gn) and np.array_equal(swc, swn)
+
+
+def test_mlp_oracle_gradient_and_product_layout():
+    """The network oracle's backward against central differences, and the
+    product's initial parameters in the oracle's layout."""
+    from oracle import mlp as OM
+    from cngi_prototype_gb300.imaging.learned_gcf import init_params
+    rng = np.random.default_rng(2)
+    p = OM.init_params(1).astype(np.float64)
+    z = rng.uniform(-1, 1, (64, 3))
+    t = rng.standard_normal(64)
+    L, g = OM.loss_grad(p, z, t)
+    for i in rng.choice(OM.N_TRAINED, 40, replace=False):
+        e = np.zeros_like(p)
+        e[i] = 1e-6
+        fd = (OM.loss_grad(p + e, z, t)[0] - OM.loss_grad(p - e, z, t)[0]) / 2e-6
+        assert abs(fd - g[i]) <= 1e-6 + 1e-5 * abs(g[i]), (i, fd, g[i])
+    q = init_params(0)
+    assert q.size == OM.NPARAM and q.dtype == np.float32
+    parts = OM.unpack(q)
+    assert np.all(parts[1] == 0) and np.all(parts[9] == 0)
+    assert np.all(parts[10][:30, 3] == 0) and np.all(parts[10][30:, :3] == 0)

@@ -49,8 +49,10 @@ def parse():
     p.add_argument('--no-e2e', action='store_true')
     p.add_argument('--no-cpu', action='store_true')
     p.add_argument('--no-err', action='store_true')
-    p.add_argument('--workload', default='large_cube', choices=['large_cube', 'mosaic'],
-                   help='large_cube (default, the headline) or mosaic (aperture-projection imaging, table GCF)')
+    p.add_argument('--workload', default='large_cube', choices=['large_cube', 'mosaic', 'standard_small', 'degrid'],
+                   help='large_cube (default, the headline), mosaic (aperture-projection imaging, table and '
+                        'learned GCF), standard_small (the small cube through the whole API), degrid (the '
+                        'differentiable degrid/grid pair)')
     p.add_argument('--mosaic-chans', type=int, default=16)
     p.add_argument('--mosaic-pointings', type=int, default=49)
     p.add_argument('--no-learned', action='store_true')
@@ -290,6 +292,178 @@ def learned_leg(args, obs, gcf, gp, vis_d, uvw_d, w_d, f_d, fidx_d, sl_d, g_tab,
     }
 
 
+def _timed(fn, steps, warmup):
+    import torch
+    for _ in range(warmup):
+        fn()
+    torch.cuda.synchronize()
+    stream = torch.cuda.current_stream()
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    e0.record(stream)
+    for _ in range(steps):
+        fn()
+    e1.record(stream)
+    torch.cuda.synchronize()
+    return e0.elapsed_time(e1) / steps
+
+
+def _line(args, world, workload, value, ms, config, roofline, cpu, e2e, err, clk, launches, extra=None):
+    line = {'metric': METRIC, 'value': value, 'unit': 'Mvis/s', 'n_gpus': world, 'steps': args.steps,
+            'warmup': args.warmup, 'ms_per_step': ms, 'higher_is_better': True, 'scaling': 'weak',
+            'vs_baseline': None, 'dtype': 'f32', 'data': 'synthetic', 'config': {'workload': workload, **config},
+            'roofline': roofline, 'cpu_baseline': cpu, 'e2e': e2e, 'err_vs_fp64': err, 'clocks': clk,
+            'gpu_launches': launches}
+    if extra:
+        line.update(extra)
+    print(json.dumps(line), flush=True)
+
+
+def run_standard_small(args, rank, world, local, dist):
+    """The small standard cube (27 antennas, 600 x 10 s, 32 channels, RR/LL,
+    512^2 at 2 arcsec, natural weighting): ngg_grid_ps device-resident, and
+    make_imaging_weight + make_psf + make_image end to end from host arrays."""
+    import torch
+    from cngi_prototype_gb300 import _lib, simulate, xds
+    from cngi_prototype_gb300.imaging import make_image, make_imaging_weight, make_psf
+    from cngi_prototype_gb300.imaging._imaging_utils import _gridding_convolutional_kernels as G
+    from cngi_prototype_gb300.imaging._imaging_utils._check_imaging_parms import _check_grid_parms
+    obs = simulate.config_standard_small(seed=1 + rank)
+    T, B, C, P = obs.vis.shape
+    gp_user = {'image_size': list(obs.image_size), 'cell_size': list(obs.cell_arcsec), 'chan_mode': 'cube',
+               'phase_center': [0.0, 0.0]}
+    gp = dict(gp_user)
+    _check_grid_parms(gp)
+    npad, cell = gp['image_size_padded'], gp['cell_size']
+    cgk = G._create_prolate_spheroidal_kernel_1D(100, 7)
+    vis_d = torch.as_tensor(obs.vis, device='cuda')
+    w_d = torch.as_tensor(obs.weight, device='cuda')
+    uvw_d = torch.as_tensor(obs.uvw, device='cuda')
+    f_d = torch.as_tensor(obs.freq, device='cuda')
+    k_d = torch.as_tensor(cgk, device='cuda')
+    grid = torch.empty((C, P, int(npad[0]), int(npad[1])), dtype=torch.complex64, device='cuda')
+    sw = torch.empty((C, P), dtype=torch.float64, device='cuda')
+    ms = _timed(lambda: _lib.grid_ps(vis_d, uvw_d, w_d, f_d, k_d, npad, cell, grid=grid, sum_weight=sw),
+                args.steps, args.warmup)
+    n_vis = T * B * C * P
+    value = n_vis * world / (ms * 1e-3) / 1e6
+    grid_bytes = C * P * int(npad[0]) * int(npad[1]) * 8
+    alg = n_vis * 12 + T * B * 24 + grid_bytes + C * P * 8
+    peak, peak_kind = measured_peaks()
+    roofline = {'bound': 'hbm', 'achieved': alg / (ms * 1e-3) / 1e9, 'peak': peak, 'unit': 'GB/s',
+                'frac': alg / (ms * 1e-3) / 1e9 / peak, 'traffic': None, 'kernel': 'ngg_grid_ps (whole call)',
+                'kernel_ms': ms, 'algorithmic_bytes': alg, 'peak_kind': peak_kind,
+                'note': 'small workload: launch- and binning-bound, not HBM-bound'}
+    # end to end: the three API calls on host numpy datasets
+    mx = xds.mxds({'xds0': xds.vis_dataset(obs.uvw, obs.vis, obs.weight, obs.freq)})
+
+    def api():
+        m2 = make_imaging_weight(mx, {'weighting': 'natural'}, gp_user, {'xds': 'xds0'})
+        im = make_psf(m2, xds.Dataset(), gp_user, {'xds': 'xds0'}, {})
+        return make_image(m2, im, gp_user, {'xds': 'xds0'}, {})
+    api()
+    torch.cuda.synchronize()
+    t0 = time.perf_counter()
+    out = api()
+    torch.cuda.synchronize()
+    te = time.perf_counter() - t0
+    e2e = {'value': n_vis / te / 1e6, 'unit': 'Mvis/s', 'h2d_bytes_per_step': int(2 * (obs.vis.nbytes +
+           obs.weight.nbytes + obs.uvw.nbytes)), 'd2h_bytes_per_step': int(2 * out['IMAGE'].values.nbytes),
+           'ms_per_step': te * 1e3, 'note': 'make_imaging_weight + make_psf + make_image, wall clock'}
+    cpu = err = None
+    if rank == 0 and not args.no_cpu:
+        from oracle import cbind
+        threads = cpu_threads()
+        go, swo, dt = oracle_sample(obs.uvw, obs.vis, obs.weight.astype(np.float64), obs.freq, cgk, npad, cell,
+                                    threads)
+        cpu = {'value': n_vis / dt / 1e6, 'unit': 'Mvis/s', 'cores': threads, 'kind': 'port',
+               'sample': f'the whole cube ({n_vis} vis), C FP64 restatement of _standard_grid_jit'}
+        corr = G._create_prolate_spheroidal_kernel(100, 7, npad)[1]
+        s0 = int(npad[0]) // 2 - obs.image_size[0] // 2
+        corr = corr[s0:s0 + obs.image_size[0], s0:s0 + obs.image_size[1]]
+        ref = np.fft.fftshift(np.fft.ifft2(np.fft.ifftshift(go, axes=(2, 3))), axes=(2, 3)).real
+        ref = ref[:, :, s0:s0 + obs.image_size[0], s0:s0 + obs.image_size[1]] * (int(npad[0]) * int(npad[1]))
+        ref = np.moveaxis(ref / np.where(swo == 0, 1, swo)[:, :, None, None], (0, 1), (2, 3)) / corr[:, :, None, None]
+        img = out['IMAGE'].values[:, :, 0]
+        ie = np.abs(img - ref)
+        err = {'image_max': float(ie.max() / np.abs(ref).max()),
+               'image_rms': float(np.sqrt(np.mean(ie ** 2)) / np.abs(ref).max()),
+               'sample': 'IMAGE of make_image (all 32 channels, both pols) vs the FP64 oracle grid + numpy FFT'}
+    if rank == 0:
+        _line(args, world, 'standard_small_natural', value, ms,
+              {'n_time': T, 'n_baseline': B, 'n_chan': C, 'n_pol': P, 'n_vis': n_vis, 'image_size': 512,
+               'grid': int(npad[0]), 'cell_arcsec': 2.0, 'weighting': 'natural', 'support': 7, 'oversampling': 100,
+               'l2': 'grid and inputs (0.5 GB) larger than L2', 'parallelism': f'replica x{world}'},
+              roofline, cpu, e2e, err, None, 11 * args.steps)
+
+
+def run_degrid(args, rank, world, local, dist):
+    """Differentiable degrid/grid pair: 2048^2 float32 model of 500 Gaussian
+    blobs (FWHM 2-20 px), 64 antennas x 992 times (2.0M rows), 64 channels
+    over 1.0-1.5 GHz, 1 pol, 1 arcsec cells. One step = model visibilities
+    (D^T, ngg_fft_correct_adjoint + ngg_degrid_ps), chi-square against
+    synthetic data (sigma 0.1), and its gradient (D, ngg_grid_ps +
+    ngg_fft_correct) through the autograd function."""
+    import torch
+    from cngi_prototype_gb300 import simulate
+    from cngi_prototype_gb300.imaging.degrid import ImagingOperator, degrid
+    rng = np.random.default_rng(3 + rank)
+    enu = simulate.log_spiral_layout(64, 2500.0, rng)
+    uvw = simulate.earth_rotation_uvw(enu, 992, 8.0)
+    T, B = uvw.shape[:2]
+    C, P, N = 64, 1, 2048
+    freq = 1.0e9 + (np.arange(C) + 0.5) * (0.5e9 / C)
+    gp = {'image_size': [N, N], 'cell_size': [1.0, 1.0], 'chan_mode': 'cube'}
+    w = torch.ones((T, B, C, P), dtype=torch.float32, device='cuda')
+    op = ImagingOperator(uvw, w, freq, gp)
+    # model: 500 Gaussians on the GPU
+    yy, xx = torch.meshgrid(torch.arange(N, device='cuda', dtype=torch.float32),
+                            torch.arange(N, device='cuda', dtype=torch.float32), indexing='ij')
+    model = torch.zeros((N, N), dtype=torch.float32, device='cuda')
+    pos = rng.uniform(0, N, (500, 2))
+    fw = rng.uniform(2, 20, 500)
+    amp = rng.uniform(0, 1, 500)
+    for k in range(500):
+        s2 = (fw[k] / 2.3548) ** 2
+        model += float(amp[k]) * torch.exp(-((xx - float(pos[k, 0])) ** 2 + (yy - float(pos[k, 1])) ** 2) / (2 * s2))
+    x = model[:, :, None, None].expand(N, N, C, P).contiguous().requires_grad_(True)
+    with torch.no_grad():
+        v_model = op.degrid(x.detach())
+        noise = torch.complex(torch.randn(v_model.shape, device='cuda'), torch.randn(v_model.shape, device='cuda'))
+        v_data = (v_model + 0.1 * noise).to(torch.complex64)
+
+    def step():
+        x.grad = None
+        r = degrid(x, op) - v_data
+        loss = (r.real ** 2 + r.imag ** 2).sum()
+        loss.backward()
+        return loss
+
+    ms = _timed(step, args.steps, args.warmup)
+    n_vis = T * B * C * P
+    value = n_vis * world / (ms * 1e-3) / 1e6
+    fwd_ms = _timed(lambda: op.degrid(x.detach()), args.steps, 1)
+    bwd_ms = _timed(lambda: op.image(v_data), args.steps, 1)
+    cpu = None
+    if rank == 0 and not args.no_cpu:
+        from cngi_prototype_gb300.imaging._imaging_utils import _gridding_convolutional_kernels as G
+        nc = min(C, cpu_threads())
+        threads = cpu_threads()
+        vs = v_data[:, :, :nc].cpu().numpy()
+        _, _, dt = oracle_sample(uvw, vs, np.ones(vs.shape), freq[:nc], G._create_prolate_spheroidal_kernel_1D(100, 7),
+                                 op.npad, op.cell, threads)
+        cpu = {'value': T * B * nc * P / dt / 1e6, 'unit': 'Mvis/s', 'cores': threads, 'kind': 'port',
+               'sample': f'the gradient half (gridding) of channels 0-{nc - 1}: C FP64 restatement of '
+                         f'_standard_grid_jit; the reference has no degridder'}
+    if rank == 0:
+        _line(args, world, 'degrid_grid_chi2_step', value, ms,
+              {'n_time': T, 'n_baseline': B, 'n_chan': C, 'n_pol': P, 'n_vis': n_vis, 'image_size': N,
+               'grid': int(op.npad[0]), 'cell_arcsec': 1.0, 'model': '500 Gaussians, FWHM 2-20 px',
+               'parallelism': f'replica x{world}'},
+              None, cpu, None, None, None, 12 * args.steps,
+              {'forward_degrid_ms': fwd_ms, 'backward_grid_ms': bwd_ms,
+               'note': 'value = model visibilities per second of one forward + chi-square + backward step'})
+
+
 def run_mosaic(args, rank, world, local, dist):
     """Mosaic aperture-projection imaging with the table GCF (one step =
     ngg_grid_gcf of the whole cube, inputs resident in HBM)."""
@@ -459,8 +633,9 @@ def main():
     from cngi_prototype_gb300.imaging._imaging_utils._check_imaging_parms import _check_grid_parms
     build.build()
     _lib.load()
-    if args.workload == 'mosaic':
-        run_mosaic(args, rank, world, local, dist)
+    if args.workload != 'large_cube':
+        {'mosaic': run_mosaic, 'standard_small': run_standard_small, 'degrid': run_degrid}[args.workload](
+            args, rank, world, local, dist)
         if dist:
             dist.barrier()
             dist.destroy_process_group()

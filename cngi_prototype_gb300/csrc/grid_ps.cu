@@ -25,8 +25,8 @@
 //  owns up to two of the 7 column residue classes (Romein's work
 //  distribution) and, for each, the 7 rows of the current footprint in
 //  registers; it adds tap*tap*datum in registers while its cells stay the
-//  same and flushes a cell to shared memory (atomic add) only when the track
-//  moves off it. Taps come from the oversampled table, loaded into shared
+//  same and flushes a cell to shared memory (atomic add) when the track
+//  moves off it or, at the latest, every second 32-step chunk. Taps come from the oversampled table, loaded into shared
 //  memory by a TMA bulk copy. Cell and oversampling indices are certified to
 //  equal the reference's FP64 results (see cell_pair).
 #include <cub/cub.cuh>
@@ -695,6 +695,16 @@ __global__ void __launch_bounds__(NW * 32, 2) k_tiles(const TileArgs a) {
                         }
                     }
                     __syncwarp();
+                }
+                // A slow track keeps adding to the same cells chunk after chunk;
+                // an FP32 running sum of hundreds of like-sized terms drifts (its
+                // rounding errors stop cancelling), so register sums are bounded
+                // to two chunks (64 steps) and the long sums run in the tile.
+                if (j & 1) {
+#pragma unroll
+                    for (int jj = 0; jj < 2; ++jj)
+#pragma unroll
+                        for (int d = 0; d < SUP; ++d) { flush_cell(jj, d); zero_cell(jj, d); }
                 }
             }
 #pragma unroll

@@ -72,6 +72,7 @@ SIGNATURES = {
     'ngg_weight_lookup': (ctypes.c_int, [ctypes.c_int, _i64, _i64, _i64, _i64, _i64, _i64,
                                          ctypes.POINTER(ctypes.c_double), _vp, _vp, _vp, _vp, _vp, _vp, _vp]),
     'ngg_fft_correct': (ctypes.c_int, [_vp, _i64, _i64, _i64, _i64, _i64, _i64, _vp, _vp, _vp, _vp]),
+    'ngg_fft_correct_f64': (ctypes.c_int, [_vp, _i64, _i64, _i64, _i64, _i64, _i64, _vp, _vp, _vp, _vp]),
     'ngg_fft_correct_adjoint': (ctypes.c_int, [_vp, ctypes.c_int, _i64, _i64, _i64, _i64, _i64, _i64,
                                                _vp, _vp, _vp, _vp]),
     'ngg_degrid_ps': (ctypes.c_int, [ctypes.POINTER(NggDegridArgs), _vp]),
@@ -248,16 +249,22 @@ def weight_lookup(uvw, weight, freq, density, factors, delta_lm, chan_mode='cube
     return out
 
 
-def fft_correct(grid_fft, sum_weight, correction, image_size):
-    """In-place inverse FFT of FFT-layout planes + crop + correction -> image (l,m,C,P) f64."""
+def fft_correct(grid_fft, sum_weight, correction, image_size, precision='single'):
+    """Inverse FFT of FFT-layout planes + crop + correction -> image (l,m,C,P) f64.
+
+    precision 'single': in-place complex64 transform (grid destroyed);
+    'double': complex128 transform in library scratch (grid kept)."""
     torch = _torch()
     n_img, P, nu, nv = grid_fft.shape
     nl, nm = int(image_size[0]), int(image_size[1])
     corr = _dev(correction, torch.float64, 'correction')
     sw = _dev(sum_weight, torch.float64, 'sum_weight')
     img = torch.empty((nl, nm, n_img, P), dtype=torch.float64, device='cuda')
-    _check(load().ngg_fft_correct(_ptr(grid_fft), n_img, P, nu, nv, nl, nm, _ptr(sw), _ptr(corr), _ptr(img),
-                                  _stream()), 'ngg_fft_correct')
+    if precision not in ('single', 'double'):
+        raise ValueError(f"precision must be 'single' or 'double', got {precision!r}")
+    name = 'ngg_fft_correct' if precision == 'single' else 'ngg_fft_correct_f64'
+    _check(getattr(load(), name)(_ptr(grid_fft), n_img, P, nu, nv, nl, nm, _ptr(sw), _ptr(corr), _ptr(img),
+                                 _stream()), name)
     return img
 
 

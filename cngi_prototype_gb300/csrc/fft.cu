@@ -13,6 +13,7 @@
 // CUFFT_INVERSE, so no scaling is applied.
 #include <cufft.h>
 
+#include <algorithm>
 #include <map>
 #include <mutex>
 #include <tuple>
@@ -26,17 +27,18 @@ struct PlanKey {
     int dev;
     int64_t nu, nv;
     int batch;
+    bool z;   // double precision (Z2Z)
     bool operator<(const PlanKey &o) const {
-        return std::tie(dev, nu, nv, batch) < std::tie(o.dev, o.nu, o.nv, o.batch);
+        return std::tie(dev, nu, nv, batch, z) < std::tie(o.dev, o.nu, o.nv, o.batch, o.z);
     }
 };
 std::mutex g_plan_mu;
 std::map<PlanKey, cufftHandle> g_plans;
 
-int get_plan(int64_t nu, int64_t nv, int batch, cufftHandle *out) {
+int get_plan(int64_t nu, int64_t nv, int batch, cufftHandle *out, bool z = false) {
     int dev = 0;
     cudaGetDevice(&dev);
-    PlanKey k{dev, nu, nv, batch};
+    PlanKey k{dev, nu, nv, batch, z};
     std::lock_guard<std::mutex> lk(g_plan_mu);
     auto it = g_plans.find(k);
     if (it != g_plans.end()) {
@@ -47,7 +49,8 @@ int get_plan(int64_t nu, int64_t nv, int batch, cufftHandle *out) {
     if (cufftCreate(&h) != CUFFT_SUCCESS) return fail(NGG_ERR_CUDA, "cufftCreate");
     long long n[2] = {(long long)nu, (long long)nv};
     size_t ws = 0;
-    cufftResult r = cufftMakePlanMany64(h, 2, n, nullptr, 1, nu * nv, nullptr, 1, nu * nv, CUFFT_C2C, batch, &ws);
+    cufftResult r = cufftMakePlanMany64(h, 2, n, nullptr, 1, nu * nv, nullptr, 1, nu * nv, z ? CUFFT_Z2Z : CUFFT_C2C, batch,
+                                        &ws);
     if (r != CUFFT_SUCCESS) {
         cufftDestroy(h);
         return fail(r == CUFFT_ALLOC_FAILED ? NGG_ERR_NOMEM : NGG_ERR_CUDA, "cufftMakePlanMany64 failed");
@@ -58,7 +61,8 @@ int get_plan(int64_t nu, int64_t nv, int batch, cufftHandle *out) {
 }
 
 // one thread per output pixel (l, m) of one plane batch
-__global__ void k_crop_correct(const float2 *planes, int nplanes, int plane0, int64_t nu, int64_t nv, int64_t nl,
+template <typename C2>
+__global__ void k_crop_correct(const C2 *planes, int nplanes, int plane0, int64_t nu, int64_t nv, int64_t nl,
                                int64_t nm, int64_t n_planes_total, const double *sum_weight,
                                const double *correction, double *image) {
     const int64_t id = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
@@ -72,8 +76,15 @@ __global__ void k_crop_correct(const float2 *planes, int nplanes, int plane0, in
         const int64_t pl = plane0 + q;
         double sw = sum_weight[pl];
         if (sw == 0.0) sw = 1.0;
-        const float re = planes[(int64_t)q * nu * nv + k1 * nv + k2].x;
-        image[id * n_planes_total + pl] = ((double)re / sw) / corr;
+        const double re = (double)planes[(int64_t)q * nu * nv + k1 * nv + k2].x;
+        image[id * n_planes_total + pl] = (re / sw) / corr;
+    }
+}
+// complex64 planes -> complex128 (exact)
+__global__ void k_widen(const float2 *src, double2 *dst, int64_t n) {
+    for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x) {
+        const float2 v = src[i];
+        dst[i] = make_double2((double)v.x, (double)v.y);
     }
 }
 // adjoint of k_crop_correct: scaled image values placed into zeroed planes
@@ -135,6 +146,46 @@ extern "C" int ngg_fft_correct(void *grid, int64_t n_img, int64_t P, int64_t nu,
             return fail(NGG_ERR_CUDA, "cufftExecC2C");
         const int64_t npx = nl * nm;
         k_crop_correct<<<(unsigned)((npx + 255) / 256), 256, 0, s>>>(base, nb, (int)p0, nu, nv, nl, nm, n_planes,
+                                                                     sum_weight, correction, image);
+        NGG_CHECK_LAUNCH("k_crop_correct");
+    }
+    return NGG_OK;
+}
+
+extern "C" int ngg_fft_correct_f64(const void *grid, int64_t n_img, int64_t P, int64_t nu, int64_t nv, int64_t nl,
+                                   int64_t nm, const double *sum_weight, const double *correction, double *image,
+                                   void *stream) {
+    clear_error();
+    cudaStream_t s = (cudaStream_t)stream;
+    if (n_img < 0 || P < 1 || nu < 1 || nv < 1 || nl < 1 || nm < 1 || nl > nu || nm > nv)
+        return fail(NGG_ERR_INVALID, "dims (need 1 <= n_l <= n_u, 1 <= n_m <= n_v)");
+    if (!grid || !sum_weight || !correction || !image) return fail(NGG_ERR_INVALID, "NULL pointer");
+    const int64_t n_planes = n_img * P;
+    if (n_planes == 0) return NGG_OK;
+    // complex128 working planes in library scratch, ~2 GB per batch
+    const int64_t plane_bytes = nu * nv * 16;
+    int64_t batch = (2ll << 30) / plane_bytes;
+    if (batch < 1) batch = 1;
+    if (batch > n_planes) batch = n_planes;
+    if (batch > 64) batch = 64;
+    ScratchList sl(s);
+    double2 *work = nullptr;
+    int rc = sl.get((void **)&work, (size_t)(batch * plane_bytes));
+    if (rc != NGG_OK) return rc;
+    const float2 *g = (const float2 *)grid;
+    for (int64_t p0 = 0; p0 < n_planes; p0 += batch) {
+        const int nb = (int)((n_planes - p0) < batch ? (n_planes - p0) : batch);
+        const int64_t n = (int64_t)nb * nu * nv;
+        k_widen<<<(unsigned)std::min<int64_t>((n + 255) / 256, 65535), 256, 0, s>>>(g + p0 * nu * nv, work, n);
+        NGG_CHECK_LAUNCH("k_widen");
+        cufftHandle h;
+        rc = get_plan(nu, nv, nb, &h, true);
+        if (rc != NGG_OK) return rc;
+        if (cufftSetStream(h, s) != CUFFT_SUCCESS) return fail(NGG_ERR_CUDA, "cufftSetStream");
+        if (cufftExecZ2Z(h, (cufftDoubleComplex *)work, (cufftDoubleComplex *)work, CUFFT_INVERSE) != CUFFT_SUCCESS)
+            return fail(NGG_ERR_CUDA, "cufftExecZ2Z");
+        const int64_t npx = nl * nm;
+        k_crop_correct<<<(unsigned)((npx + 255) / 256), 256, 0, s>>>(work, nb, (int)p0, nu, nv, nl, nm, n_planes,
                                                                      sum_weight, correction, image);
         NGG_CHECK_LAUNCH("k_crop_correct");
     }

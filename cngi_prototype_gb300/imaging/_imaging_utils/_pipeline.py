@@ -36,8 +36,12 @@ def chan_chunks(n_chan, n_pol, npad, chan_mode, budget=GRID_BUDGET_BYTES):
     return [(c0, min(n_chan, c0 + k)) for c0 in range(0, n_chan, k)]
 
 
-def image_cube(vis, uvw, imaging_weight, freq, grid_parms, do_psf):
-    """Dirty image or PSF (N0, N1, C_img, P) float64 and sum_weight (C_img, P)."""
+def image_cube(vis, uvw, imaging_weight, freq, grid_parms, do_psf, normalize=True):
+    """Dirty image or PSF (N0, N1, C_img, P) float64 and sum_weight (C_img, P).
+
+    normalize=False leaves out the division by sum_weight (the image is
+    Re(FFT^-1 grid) * Nu*Nv / correction): partial images of disjoint row
+    sets then add up to the image of their union times its sum_weight."""
     import torch
     npad = np.asarray(grid_parms['image_size_padded'])
     image_size = np.asarray(grid_parms['image_size'])
@@ -63,7 +67,8 @@ def image_cube(vis, uvw, imaging_weight, freq, grid_parms, do_psf):
             vv = _slice_chan(v, c0, c1) if (c0, c1) != (0, C) else v
         g, sw = _lib.grid_ps(vv, uvw_d, wv, freq[c0:c1], cgk_d, npad, cell, mode='psf' if do_psf else 'data',
                              chan_mode=chan_mode, layout='fft', support=SUPPORT, oversampling=OVERSAMPLING)
-        img = _lib.fft_correct(g, sw, corr_d, image_size)
+        img = _lib.fft_correct(g, sw if normalize else torch.ones_like(sw), corr_d, image_size,
+                               precision=grid_parms.get('fft_precision', 'single'))
         del g
         if chan_mode == 'continuum':
             image[:, :, 0:1] = img.cpu().numpy()
@@ -74,8 +79,12 @@ def image_cube(vis, uvw, imaging_weight, freq, grid_parms, do_psf):
     return image, sum_weight
 
 
-def imaging_weights(uvw, weight, freq, grid_parms, imaging_weights_parms):
-    """Uniform/Briggs imaging weights (T,B,C,P) float32 on the GPU (torch tensor)."""
+def imaging_weights(uvw, weight, freq, grid_parms, imaging_weights_parms, density_reduce=None):
+    """Uniform/Briggs imaging weights (T,B,C,P) float32 on the GPU (torch tensor).
+
+    density_reduce(density, sum_weight) -> (density, sum_weight), when given,
+    replaces the local weight-density grid and its sum before the Briggs
+    factors are taken (the sum over row shards in continuum mode)."""
     import torch
     cell = np.asarray(grid_parms['cell_size'], dtype=np.float64)
     image_size = np.asarray(grid_parms['image_size'])
@@ -84,6 +93,8 @@ def imaging_weights(uvw, weight, freq, grid_parms, imaging_weights_parms):
     w_d = _lib._dev(_arr(weight), torch.float32, 'weight')
     f_d = _lib._dev(np.asarray(freq, dtype=np.float64), torch.float64, 'freq')
     dens, dsw = _lib.grid_density(uvw_d, w_d, f_d, image_size, cell, chan_mode)
+    if density_reduce is not None:
+        dens, dsw = density_reduce(dens, dsw)
     fac = _lib.briggs_factors(dens, dsw, imaging_weights_parms['weighting'], imaging_weights_parms.get('robust', 0.5),
                               imaging_weights_parms.get('briggs_abs_noise', 1.0))
     return _lib.weight_lookup(uvw_d, w_d, f_d, dens, fac, cell, chan_mode)

@@ -7,7 +7,7 @@ import numpy as np
 
 from ..xds import set_var
 from ._imaging_utils._check_imaging_parms import _check_grid_parms
-from ._imaging_utils._pipeline import image_cube
+from ._imaging_utils import _pipeline
 from ._imaging_utils._sel import _check_sel_parms, _register_group
 
 
@@ -24,7 +24,7 @@ def _image_coords(img_xds, grid_parms, vis, chan_mode):
     return img_xds.assign_coords(coords)
 
 
-def _make(vis_mxds, img_xds, grid_parms, vis_sel_parms, img_sel_parms, do_psf):
+def _make(vis_mxds, img_xds, grid_parms, vis_sel_parms, img_sel_parms, do_psf, cube_fn=None):
     _mxds = vis_mxds.copy(deep=False)
     _img = img_xds.copy(deep=False)
     _vsp = copy.deepcopy(vis_sel_parms)
@@ -39,7 +39,8 @@ def _make(vis_mxds, img_xds, grid_parms, vis_sel_parms, img_sel_parms, do_psf):
     gin, gout = _vsp['data_group_in'], _isp['data_group_out']
     iw_name = gin.get('imaging_weight', gin.get('weight'))
     vis = None if do_psf else _vis[gin['data']]
-    image, sw = image_cube(vis, _vis[gin['uvw']], _vis[iw_name], _vis.coords['chan'].values, _gp, do_psf)
+    cube_fn = cube_fn or _pipeline.image_cube
+    image, sw = cube_fn(vis, _vis[gin['uvw']], _vis[iw_name], _vis.coords['chan'].values, _gp, do_psf)
     _img = _image_coords(_img, _gp, _vis, _gp['chan_mode'])
     set_var(_img, gout['sum_weight'], sw[None, :, :], ('time', 'chan', 'pol'))
     set_var(_img, gout['psf' if do_psf else 'image'], image[:, :, None, :, :], ('l', 'm', 'time', 'chan', 'pol'))

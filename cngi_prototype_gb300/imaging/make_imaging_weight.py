@@ -5,7 +5,7 @@ import copy
 
 from ..xds import set_var
 from ._imaging_utils._check_imaging_parms import _check_grid_parms, _check_imaging_weights_parms
-from ._imaging_utils._pipeline import imaging_weights
+from ._imaging_utils import _pipeline
 from ._imaging_utils._sel import _check_sel_parms, _register_group
 
 
@@ -17,6 +17,10 @@ def make_imaging_weight(vis_mxds, imaging_weights_parms, grid_parms, sel_parms):
     the weight density on the unpadded grid and divide each weight by
     f0*W+f1 at its cell. Inputs are not modified; a new mxds is returned.
     """
+    return _make_imaging_weight(vis_mxds, imaging_weights_parms, grid_parms, sel_parms)
+
+
+def _make_imaging_weight(vis_mxds, imaging_weights_parms, grid_parms, sel_parms, density_reduce=None):
     _mxds = vis_mxds.copy(deep=False)
     _iwp = copy.deepcopy(imaging_weights_parms)
     _gp = copy.deepcopy(grid_parms)
@@ -34,7 +38,8 @@ def make_imaging_weight(vis_mxds, imaging_weights_parms, grid_parms, sel_parms):
         _register_group(_vis, gout)
         return _mxds
     assert _check_grid_parms(_gp), '######### ERROR: grid_parms checking failed'
-    iw = imaging_weights(_vis[gin['uvw']], _vis[gin['weight']], _vis.coords['chan'].values, _gp, _iwp)
+    iw = _pipeline.imaging_weights(_vis[gin['uvw']], _vis[gin['weight']], _vis.coords['chan'].values, _gp, _iwp,
+                                   density_reduce=density_reduce)
     set_var(_vis, gout['imaging_weight'], iw.cpu().numpy(), _vis[gin['weight']].dims)
     _register_group(_vis, gout)
     return _mxds

@@ -155,6 +155,18 @@ int ngg_fft_correct(void *grid, int64_t n_chan_img, int64_t n_pol,
                     const double *sum_weight, const double *correction, double *image,
                     void *stream);
 
+/* As ngg_fft_correct with the inverse transform in double precision
+ * (complex128 working planes in library scratch; grid is left unchanged).
+ * The FP32 transform's rounding, amplified by 1/correction towards the image
+ * edge (the correction falls to ~1.5e-3 in the corners), puts a floor of
+ * ~6e-6 of the peak under the image error; this variant removes it at
+ * ~15-25x the transform time (GB300 executes FP64 at a small fraction of
+ * its FP32 rate). Same reference lines as ngg_fft_correct. */
+int ngg_fft_correct_f64(const void *grid, int64_t n_chan_img, int64_t n_pol,
+                        int64_t n_u, int64_t n_v, int64_t n_l, int64_t n_m,
+                        const double *sum_weight, const double *correction, double *image,
+                        void *stream);
+
 /* ---- degridding: the exact adjoint of the imaging operator ---------------
  * The reference has no visibility degridder (_graph_standard_degrid prints
  * "Degridding of visibilities and psf still needs to be implemented",

@@ -39,6 +39,21 @@ def test_make_image_and_psf(ngg, name):
     assert 'IMAGE' not in mx.attrs['xds0'] and 'data_groups' not in img.attrs or True
 
 
+@pytest.mark.parametrize('name', ['std_cube', 'std_odd'])
+def test_make_image_double_precision_fft(ngg, name):
+    """fft_precision 'double' runs the inverse transform in complex128: the
+    image then differs from the reference only by the FP32 gridding error."""
+    from cngi_prototype_gb300 import xds
+    from cngi_prototype_gb300.imaging import make_image
+    d = load_golden(name)
+    mx = _mx(d)
+    single = make_image(mx, xds.Dataset(), _gp(d), {'xds': 'xds0'}, {})['IMAGE'].values[:, :, 0]
+    gp = dict(_gp(d), fft_precision='double')
+    double = make_image(mx, xds.Dataset(), gp, {'xds': 'xds0'}, {})['IMAGE'].values[:, :, 0]
+    e1, e2 = _err(single, d['image']), _err(double, d['image'])
+    assert e2 < 1e-5 and e2 <= e1 * 1.01 + 1e-9, (e1, e2)
+
+
 @pytest.mark.parametrize('weighting,robust', [('briggs', 0.5), ('uniform', 0.0), ('briggs', -1.3)])
 def test_make_imaging_weight(ngg, weighting, robust):
     from cngi_prototype_gb300.imaging import make_imaging_weight

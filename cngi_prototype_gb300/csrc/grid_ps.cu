@@ -139,16 +139,16 @@ struct PackArgs {
 // channels x 32 steps of one (baseline, chunk): the reads are contiguous over
 // channels, a shared-memory transpose makes the writes contiguous over time.
 template <int NP, bool CPLX>
-__global__ void __launch_bounds__(1024) k_pack(const PackArgs a) {
+__global__ void __launch_bounds__(256) k_pack(const PackArgs a) {
     __shared__ uint2 s_meta[32][33];
     __shared__ float4 s_wv[32][33];
     __shared__ float s_sw[NP][32][33];
-    const int x = threadIdx.x, y = threadIdx.y;
+    const int x = threadIdx.x;
     const int64_t b = blockIdx.x;
     const int k = blockIdx.y;
     const int64_t c0 = (int64_t)blockIdx.z * 32;
     const int cu_c = (int)(a.nu / 2), cv_c = (int)(a.nv / 2);
-    {
+    for (int y = threadIdx.y; y < 32; y += 8) {
         const int64_t c = c0 + x, t = (int64_t)k * CH + y;
         uint2 meta = make_uint2(NO_CELL, 0u);
         float4 wv = make_float4(0.f, 0.f, 0.f, 0.f);
@@ -209,17 +209,19 @@ __global__ void __launch_bounds__(1024) k_pack(const PackArgs a) {
         for (int p = 0; p < NP; ++p) s_sw[p][x][y] = swc[p];
     }
     __syncthreads();
-    // warp y writes channel c0 + y, lane x its step x
-    const int64_t c = c0 + y;
-    if (c >= a.C) return;
-    const int64_t ri = ((c * a.B + b) * a.nk + k) * CH + x;
-    a.meta[ri] = s_meta[y][x];
-    a.wvp[ri] = s_wv[y][x];
+    // warp w writes channels c0 + w + 8i, lane x its step x
+    for (int y = threadIdx.y; y < 32; y += 8) {
+        const int64_t c = c0 + y;
+        if (c >= a.C) break;
+        const int64_t ri = ((c * a.B + b) * a.nk + k) * CH + x;
+        a.meta[ri] = s_meta[y][x];
+        a.wvp[ri] = s_wv[y][x];
 #pragma unroll
-    for (int p = 0; p < NP; ++p) {
-        float v = s_sw[p][y][x];
-        for (int o = 16; o > 0; o >>= 1) v += __shfl_xor_sync(0xffffffffu, v, o);
-        if (x == 0) a.sw_part[((c * NP + p) * a.B + b) * a.nk + k] = (double)v;
+        for (int p = 0; p < NP; ++p) {
+            float v = s_sw[p][y][x];
+            for (int o = 16; o > 0; o >>= 1) v += __shfl_xor_sync(0xffffffffu, v, o);
+            if (x == 0) a.sw_part[((c * NP + p) * a.B + b) * a.nk + k] = (double)v;
+        }
     }
 }
 
@@ -467,6 +469,78 @@ __global__ void k_zero_split(const int64_t *bin_start, const int *bbox, int n_im
     }
 }
 
+constexpr int ZBUF = 2048;   // bytes of zeros in shared memory: the source of the zero-fill bulk stores
+constexpr int ZPER = 4;      // zero-fill row blocks issued per tile item taken
+
+// Zero nbytes of the grid at gp (gp and nbytes multiples of elem): plain
+// stores up to the first 16-byte boundary and after the last one, TMA bulk
+// stores (asynchronous; committed by the caller) from the zero buffer at
+// shared address zs for the aligned middle.
+__device__ __forceinline__ void zero_fill(char *gp, int64_t nbytes, unsigned zs, int elem) {
+    while (nbytes > 0 && ((uintptr_t)gp & 15)) {
+        if (elem == 8) *reinterpret_cast<float2 *>(gp) = make_float2(0.f, 0.f);
+        else *reinterpret_cast<float *>(gp) = 0.f;
+        gp += elem;
+        nbytes -= elem;
+    }
+    const int64_t mid = nbytes & ~(int64_t)15;
+    for (char *q = gp + mid; q < gp + nbytes; q += elem) {
+        if (elem == 8) *reinterpret_cast<float2 *>(q) = make_float2(0.f, 0.f);
+        else *reinterpret_cast<float *>(q) = 0.f;
+    }
+    for (int64_t o = 0; o < mid; o += ZBUF) {
+        const unsigned sz = (unsigned)(mid - o < ZBUF ? mid - o : ZBUF);
+        asm volatile("cp.async.bulk.global.shared::cta.bulk_group [%0], [%1], %2;" ::"l"(gp + o), "r"(zs), "r"(sz)
+                     : "memory");
+    }
+}
+
+struct ZeroRows {
+    void *grid;
+    int64_t nu, nv, P;
+    int p0, nrb;
+    int64_t n_items;
+    int R0, R1, V0, V1, cu_c, cv_c;   // busy box rows/columns (natural order), grid centre
+    unsigned zs;                       // shared address of the zero buffer
+    int *counter;
+};
+
+// Take the next block of ZR rows outside the busy box and zero it (the part
+// of each row outside the box, in stored order); false when none is left.
+template <int NP, int ELEM, bool FFTL>
+__device__ __noinline__ bool zero_next(const ZeroRows &z) {
+    constexpr int ZR = 8;
+    const long long it = atomicAdd(z.counter, 1);
+    if (it >= z.n_items) return false;
+    const int64_t q = it / z.nrb;
+    const int rb = (int)(it % z.nrb);
+    const int cimg = (int)(q / NP), p = (int)(q % NP);
+    const int64_t pbase = ((int64_t)cimg * z.P + z.p0 + p) * z.nu * z.nv;
+    const int r_end = min(rb * ZR + ZR, (int)z.nu);
+    for (int r = rb * ZR; r < r_end; ++r) {
+        const int un = FFTL ? (r + z.cu_c >= z.nu ? r + z.cu_c - (int)z.nu : r + z.cu_c) : r;   // natural row
+        char *row = reinterpret_cast<char *>(z.grid) + (pbase + (int64_t)r * z.nv) * ELEM;
+        if (!(un >= z.R0 && un < z.R1 && z.V1 > z.V0)) {
+            zero_fill(row, z.nv * ELEM, z.zs, ELEM);
+            continue;
+        }
+        // stored columns of the natural busy range [V0, V1)
+        int s0 = z.V0;
+        const int L = z.V1 - z.V0;
+        if (FFTL) { s0 = z.V0 - z.cv_c; if (s0 < 0) s0 += (int)z.nv; }
+        if (s0 + L <= z.nv) {
+            zero_fill(row, (int64_t)s0 * ELEM, z.zs, ELEM);
+            zero_fill(row + (int64_t)(s0 + L) * ELEM, (z.nv - s0 - L) * ELEM, z.zs, ELEM);
+        } else {
+            const int e = s0 + L - (int)z.nv;
+            zero_fill(row + (int64_t)e * ELEM, (int64_t)(s0 - e) * ELEM, z.zs, ELEM);
+        }
+    }
+    asm volatile("cp.async.bulk.commit_group;" ::: "memory");
+    asm volatile("cp.async.bulk.wait_group.read 32;" ::: "memory");   // bound the stores in flight
+    return true;
+}
+
 // register accumulator of one (column, row) cell
 template <bool CPLX>
 struct Cell;
@@ -484,16 +558,18 @@ __global__ void __launch_bounds__(NW * 32, 2) k_tiles(const TileArgs a) {
     float *acc_s = reinterpret_cast<float *>(smem);
     const size_t acc_bytes = (size_t)NP * TU * TV * ACC_ELEM;
     float *tab = reinterpret_cast<float *>(smem + acc_bytes);
-    float *nsum = tab + ((a.tab_bytes + 3) / 4);
-    const int nsum_len = a.os + 1;
-    float4 *rec_wv = reinterpret_cast<float4 *>(nsum + ((nsum_len + 3) & ~3));
-    float4 *rec_tv = rec_wv + NW * NREC;              // 2 per record
+    // per warp: the round's step records (taps, cell, info) and, double
+    // buffered, the packed steps of this round and the next (cp.async)
+    float4 *rec_tv = reinterpret_cast<float4 *>(tab + ((a.tab_bytes + 3) / 4));   // 2 per record
     unsigned *rec_cuv = reinterpret_cast<unsigned *>(rec_tv + 2 * NW * NREC);
     int *rec_info = reinterpret_cast<int *>(rec_cuv + NW * NREC);
     int4 *ginfo = reinterpret_cast<int4 *>(rec_info + NW * NREC);   // (c, b, t0, valid) per group
-    double *sw_part = reinterpret_cast<double *>(ginfo + NW * NG);
-    unsigned long long *mbar = reinterpret_cast<unsigned long long *>(sw_part + NW * 4);
+    float4 *raw_wv = reinterpret_cast<float4 *>(ginfo + NW * NG);    // [NW][2][NREC]
+    uint2 *raw_meta = reinterpret_cast<uint2 *>(raw_wv + NW * 2 * NREC);
+    unsigned long long *mbar = reinterpret_cast<unsigned long long *>(raw_meta + NW * 2 * NREC);
     int *s_item = reinterpret_cast<int *>(mbar + 1);   // [kind, item]
+    float4 *zbuf = reinterpret_cast<float4 *>(
+        (reinterpret_cast<uintptr_t>(s_item + 2) + 15) & ~static_cast<uintptr_t>(15));
 
     const int tid = threadIdx.x;
     const int warp = tid >> 5, lane = tid & 31;
@@ -520,7 +596,10 @@ __global__ void __launch_bounds__(NW * 32, 2) k_tiles(const TileArgs a) {
     }
     __syncthreads();
     for (int i = tid; i < NP * TU * TV * (CPLX ? 2 : 1); i += blockDim.x) acc_s[i] = 0.f;
+    for (int i = tid; i < ZBUF / 16; i += blockDim.x) zbuf[i] = make_float4(0.f, 0.f, 0.f, 0.f);
+    asm volatile("fence.proxy.async.shared::cta;" ::: "memory");   // the bulk stores read zbuf
     __syncthreads();
+    const unsigned zs = (unsigned)__cvta_generic_to_shared(zbuf);
 
     const int64_t NT = (int64_t)a.ntu * a.ntv;
     const int cu_c = (int)(a.nu / 2), cv_c = (int)(a.nv / 2);
@@ -535,61 +614,32 @@ __global__ void __launch_bounds__(NW * 32, 2) k_tiles(const TileArgs a) {
     constexpr int ZR = 8;
     const int nrb = (int)((a.nu + ZR - 1) / ZR);
     const int64_t n_zero_items = (int64_t)a.n_img * NP * nrb;
-    const int order0 = blockIdx.x & 1;   // odd CTAs start with zero rows
-    int stage = 0;
 
     int4 *my_ginfo = ginfo + warp * NG;
     unsigned *my_cuv = rec_cuv + warp * NREC;
     int *my_info = rec_info + warp * NREC;
-    float4 *my_wv = rec_wv + warp * NREC;
     float4 *my_tv = rec_tv + 2 * warp * NREC;
+    float4 *my_raw_wv = raw_wv + warp * 2 * NREC;
+    uint2 *my_raw_meta = raw_meta + warp * 2 * NREC;
 
+    // Rows outside the busy box are zeroed by TMA bulk stores that thread 0
+    // issues between tile items (ZPER row blocks per item, the rest after the
+    // last one): the grid write they carry overlaps the tile work instead of
+    // taking CTAs away from it.
+    const ZeroRows zr{a.grid, a.nu, a.nv, a.P, a.p0, nrb, n_zero_items, R0, R1, V0, V1, cu_c, cv_c, zs,
+                      &a.work_counter[1]};
+    bool zero_left = true;   // thread 0: zero row blocks remain
     for (;;) {
         if (tid == 0) {
-            int kind = -1;
-            long long it = 0;
-            while (stage < 2) {
-                const int which = stage == 0 ? order0 : 1 - order0;
-                if (which == 0) {
-                    it = atomicAdd(&a.work_counter[0], 1);
-                    if (it < n_tile_items) { kind = 0; break; }
-                } else {
-                    it = atomicAdd(&a.work_counter[1], 1);
-                    if (it < n_zero_items) { kind = 1; break; }
-                }
-                ++stage;
-            }
-            s_item[0] = kind;
+            const long long it = atomicAdd(&a.work_counter[0], 1);
+            s_item[0] = it < n_tile_items ? 0 : -1;
             s_item[1] = (int)it;
+            for (int z = 0; z < ZPER && zero_left; ++z) zero_left = zero_next<NP, (CPLX || FFTL) ? 8 : 4, FFTL>(zr);
         }
         __syncthreads();
         const int kind = s_item[0];
         const int64_t item = s_item[1];
         if (kind < 0) break;
-        if (kind == 1) {
-            // ---------------- zero rows outside the busy box ----------------
-            const int64_t q = item / nrb;
-            const int rb = (int)(item % nrb);
-            const int cimg = (int)(q / NP), p = (int)(q % NP);
-            const int64_t pbase = ((int64_t)cimg * a.P + a.p0 + p) * plane;
-            const int r_end = min(rb * ZR + ZR, (int)a.nu);
-            for (int r = rb * ZR; r < r_end; ++r) {
-                int un = r;
-                if (FFTL) un = r + cu_c >= a.nu ? r + cu_c - (int)a.nu : r + cu_c;   // natural row
-                const bool in_band = un >= R0 && un < R1;
-                for (int dv = tid; dv < a.nv; dv += blockDim.x) {
-                    int vn = dv;
-                    if (FFTL) vn = dv + cv_c >= a.nv ? dv + cv_c - (int)a.nv : dv + cv_c;
-                    if (!in_band || vn < V0 || vn >= V1) {
-                        const int64_t off = pbase + (int64_t)r * a.nv + dv;
-                        if (CPLX || FFTL) reinterpret_cast<float2 *>(a.grid)[off] = make_float2(0.f, 0.f);
-                        else reinterpret_cast<float *>(a.grid)[off] = 0.f;
-                    }
-                }
-            }
-            __syncthreads();
-            continue;
-        }
         const SubItem si = a.subs[item];
         int tiu, tiv, cimg;
         int64_t bin;
@@ -650,8 +700,8 @@ __global__ void __launch_bounds__(NW * 32, 2) k_tiles(const TileArgs a) {
                 if constexpr (CPLX) acc[j][d].b = make_float2(0.f, 0.f);
             };
 
-            for (int j = 0; j < jmax; ++j) {
-                // decode the chunk of each group once
+            // chunk j of each group -> my_ginfo (lanes 0..NG-1)
+            auto decode = [&](int j) {
                 if (lane < NG) {
                     const int ggi = warp * NG + lane;
                     const int64_t grs = e0 + (n * ggi) / (NW * NG);
@@ -667,45 +717,78 @@ __global__ void __launch_bounds__(NW * 32, 2) k_tiles(const TileArgs a) {
                     my_ginfo[lane] = gi4;
                 }
                 __syncwarp();
+            };
+            // start the copies of round rnd of the current chunks into buffer buf:
+            // each lane its two packed steps (meta 8 bytes, data 16 bytes)
+            auto prefetch = [&](int rnd, int buf) {
+#pragma unroll
+                for (int k2 = 0; k2 < 2; ++k2) {
+                    // record q = s*NG + gg: the processors' records of one step are adjacent
+                    const int r = lane + 32 * k2;
+                    const int gg = r % NG, s = r / NG;
+                    const int4 gi4 = my_ginfo[gg];
+                    uint2 *dm = my_raw_meta + buf * NREC + r;
+                    if (gi4.w) {
+                        const int64_t ri = ((int64_t)gi4.x * a.B + gi4.y) * ((int64_t)a.nk * CH) + gi4.z +
+                                           rnd * ROUND + s;
+                        asm volatile("cp.async.ca.shared.global [%0], [%1], 8;" ::"r"(
+                                         (unsigned)__cvta_generic_to_shared(dm)),
+                                     "l"(a.meta + ri)
+                                     : "memory");
+                        asm volatile("cp.async.cg.shared.global [%0], [%1], 16;" ::"r"(
+                                         (unsigned)__cvta_generic_to_shared(my_raw_wv + buf * NREC + r)),
+                                     "l"(a.wvp + ri)
+                                     : "memory");
+                    } else {
+                        *dm = make_uint2(NO_CELL, 0u);
+                    }
+                }
+            };
+            if (jmax > 0) {
+                decode(0);
+                prefetch(0, 0);
+            }
+            asm volatile("cp.async.commit_group;" ::: "memory");
+
+            for (int j = 0; j < jmax; ++j) {
                 for (int rnd = 0; rnd < CH / ROUND; ++rnd) {
-                    // ---- producer: 2 records per lane ----
+                    const int buf = rnd & 1;   // CH / ROUND is even: round parity continues across chunks
+                    // copies of the next round overlap this one
+                    if (rnd + 1 < CH / ROUND) {
+                        prefetch(rnd + 1, buf ^ 1);
+                    } else if (j + 1 < jmax) {
+                        decode(j + 1);
+                        prefetch(0, buf ^ 1);
+                    }
+                    asm volatile("cp.async.commit_group;" ::: "memory");
+                    asm volatile("cp.async.wait_group 1;" ::: "memory");   // this round's copies are in
+                    // ---- producer: taps of this lane's two steps ----
 #pragma unroll
                     for (int k2 = 0; k2 < 2; ++k2) {
                         const int r = lane + 32 * k2;
-                        const int gg = r / ROUND, s = r % ROUND;
-                        const int4 gi4 = my_ginfo[gg];
+                        const uint2 m = my_raw_meta[buf * NREC + r];
                         unsigned cuv = 0;
                         int info = 0;
-                        float4 wv = make_float4(0.f, 0.f, 0.f, 0.f);
                         float4 tva = make_float4(0.f, 0.f, 0.f, 0.f), tvb = tva;
-                        if (gi4.w) {
-                            // the packed step (t = t0 + rnd*ROUND + s; chunk padding is packed as empty)
-                            const int64_t ri = ((int64_t)gi4.x * a.B + gi4.y) * ((int64_t)a.nk * CH) + gi4.z +
-                                               rnd * ROUND + s;
-                            const uint2 m = a.meta[ri];
-                            if (m.x != NO_CELL) {
-                                wv = a.wvp[ri];
-                                const int ou = (int)(m.y & 0xffffu) - 32768, ov = (int)(m.y >> 16) - 32768;
-                                cuv = m.x;
-                                info = 1 | ((ou + 1024) << 1);
-                                float tv[SUP];
+                        if (m.x != NO_CELL) {
+                            const int ou = (int)(m.y & 0xffffu) - 32768, ov = (int)(m.y >> 16) - 32768;
+                            cuv = m.x;
+                            info = 1 | ((ou + 1024) << 1);
+                            float tv[SUP];
 #pragma unroll
-                                for (int d = 0; d < SUP; ++d) tv[d] = tab[abs(a.os * (d - SC) + ov)];
-                                tva = make_float4(tv[0], tv[1], tv[2], tv[3]);
-                                tvb = make_float4(tv[4], tv[5], tv[6], 0.f);
-                            }
+                            for (int d = 0; d < SUP; ++d) tv[d] = tab[abs(a.os * (d - SC) + ov)];
+                            tva = make_float4(tv[0], tv[1], tv[2], tv[3]);
+                            tvb = make_float4(tv[4], tv[5], tv[6], 0.f);
                         }
-                        const int ri = gg * ROUND + s;
-                        my_cuv[ri] = cuv;
-                        my_info[ri] = info;
-                        my_wv[ri] = wv;
-                        my_tv[2 * ri] = tva;
-                        my_tv[2 * ri + 1] = tvb;
+                        my_cuv[r] = cuv;
+                        my_info[r] = info;
+                        my_tv[r] = tva;
+                        my_tv[NREC + r] = tvb;
                     }
                     __syncwarp();
                     // ---- consumer: ROUND steps of this processor's chunk ----
                     for (int s = 0; s < ROUND; ++s) {
-                        const int ri = g * ROUND + s;
+                        const int ri = s * NG + g;
                         const int info = my_info[ri];
                         if (!(info & 1)) continue;
                         const unsigned cuv = my_cuv[ri];
@@ -759,8 +842,8 @@ __global__ void __launch_bounds__(NW * 32, 2) k_tiles(const TileArgs a) {
                                 }
                             }
                         }
-                        const float4 wv = my_wv[ri];
-                        const float4 tva = my_tv[2 * ri], tvb = my_tv[2 * ri + 1];
+                        const float4 wv = my_raw_wv[buf * NREC + ri];
+                        const float4 tva = my_tv[ri], tvb = my_tv[NREC + ri];
                         const float tv[SUP] = {tva.x, tva.y, tva.z, tva.w, tvb.x, tvb.y, tvb.z};
 #pragma unroll
                         for (int jj = 0; jj < 2; ++jj) {
@@ -848,16 +931,21 @@ __global__ void __launch_bounds__(NW * 32, 2) k_tiles(const TileArgs a) {
         }
         __syncthreads();
     }
+    if (tid == 0) {
+        while (zero_left) zero_left = zero_next<NP, (CPLX || FFTL) ? 8 : 4, FFTL>(zr);
+        asm volatile("cp.async.bulk.wait_group 0;" ::: "memory");   // the zero rows are written
+    }
 }
 
 size_t tile_smem_bytes(int np, bool cplx, int tab_bytes, int os) {
     size_t acc = (size_t)np * TU * TV * (cplx ? 8 : 4);
     size_t tab = (size_t)((tab_bytes + 3) / 4) * 4;
-    size_t ns = (size_t)(((os + 1) + 3) & ~3) * 4;
-    size_t rec = (size_t)NW * NG * ROUND * (16 + 32 + 4 + 4);
+    size_t rec = (size_t)NW * NG * ROUND * (32 + 4 + 4);       // taps, cell, info
+    size_t raw = (size_t)NW * 2 * NG * ROUND * (16 + 8);       // packed steps, two rounds
     size_t gin = (size_t)NW * NG * 16;
-    size_t misc = NW * 4 * 8 + 8 + 16;
-    return acc + tab + ns + rec + gin + misc;
+    size_t misc = 8 + 8;
+    (void)os;
+    return acc + tab + rec + gin + raw + misc + 16 + ZBUF;
 }
 
 template <int NP, bool CPLX, bool FFTL>
@@ -1161,7 +1249,7 @@ extern "C" int ngg_grid_ps(const NggGridArgs *a, void *stream) {
             pa.T = T; pa.B = B; pa.C = C; pa.P = P;
             pa.nu = nu; pa.nv = nv;
             pa.nk = nk; pa.p0 = (int)p0; pa.os = a->oversampling;
-            const dim3 pg((unsigned)B, (unsigned)nk, (unsigned)((C + 31) / 32)), pb(32, 32);
+            const dim3 pg((unsigned)B, (unsigned)nk, (unsigned)((C + 31) / 32)), pb(32, 8);
             if (np == 2) {
                 if (cplx) k_pack<2, true><<<pg, pb, 0, s>>>(pa); else k_pack<2, false><<<pg, pb, 0, s>>>(pa);
             } else {

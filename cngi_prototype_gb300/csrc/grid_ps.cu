@@ -470,7 +470,6 @@ __global__ void k_zero_split(const int64_t *bin_start, const int *bbox, int n_im
 }
 
 constexpr int ZBUF = 2048;   // bytes of zeros in shared memory: the source of the zero-fill bulk stores
-constexpr int ZPER = 4;      // zero-fill row blocks issued per tile item taken
 
 // Zero nbytes of the grid at gp (gp and nbytes multiples of elem): plain
 // stores up to the first 16-byte boundary and after the last one, TMA bulk
@@ -622,19 +621,18 @@ __global__ void __launch_bounds__(NW * 32, 2) k_tiles(const TileArgs a) {
     float4 *my_raw_wv = raw_wv + warp * 2 * NREC;
     uint2 *my_raw_meta = raw_meta + warp * 2 * NREC;
 
-    // Rows outside the busy box are zeroed by TMA bulk stores that thread 0
-    // issues between tile items (ZPER row blocks per item, the rest after the
-    // last one): the grid write they carry overlaps the tile work instead of
-    // taking CTAs away from it.
+    // Rows outside the busy box are zeroed by TMA bulk stores that lane 0 of
+    // each warp issues, one block of rows at a time, just before the warp
+    // waits at a tile barrier (the rest after the last tile): the grid write
+    // they carry overlaps the tile work instead of taking CTAs away from it.
     const ZeroRows zr{a.grid, a.nu, a.nv, a.P, a.p0, nrb, n_zero_items, R0, R1, V0, V1, cu_c, cv_c, zs,
                       &a.work_counter[1]};
-    bool zero_left = true;   // thread 0: zero row blocks remain
+    bool zero_left = lane == 0;   // this warp's issuing lane: zero row blocks remain
     for (;;) {
         if (tid == 0) {
             const long long it = atomicAdd(&a.work_counter[0], 1);
             s_item[0] = it < n_tile_items ? 0 : -1;
             s_item[1] = (int)it;
-            for (int z = 0; z < ZPER && zero_left; ++z) zero_left = zero_next<NP, (CPLX || FFTL) ? 8 : 4, FFTL>(zr);
         }
         __syncthreads();
         const int kind = s_item[0];
@@ -884,6 +882,7 @@ __global__ void __launch_bounds__(NW * 32, 2) k_tiles(const TileArgs a) {
             for (int jj = 0; jj < 2; ++jj)
 #pragma unroll
                 for (int d = 0; d < SUP; ++d) flush_cell(jj, d);
+            if (zero_left) zero_left = zero_next<NP, (CPLX || FFTL) ? 8 : 4, FFTL>(zr);
             __syncthreads();   // every warp's cells are in the tile
         }
 
@@ -929,9 +928,10 @@ __global__ void __launch_bounds__(NW * 32, 2) k_tiles(const TileArgs a) {
                 }
             }
         }
+        if (zero_left) zero_left = zero_next<NP, (CPLX || FFTL) ? 8 : 4, FFTL>(zr);
         __syncthreads();
     }
-    if (tid == 0) {
+    if (lane == 0) {
         while (zero_left) zero_left = zero_next<NP, (CPLX || FFTL) ? 8 : 4, FFTL>(zr);
         asm volatile("cp.async.bulk.wait_group 0;" ::: "memory");   // the zero rows are written
     }

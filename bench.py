@@ -727,11 +727,15 @@ def main():
     if os.path.exists(tr_path):
         try:
             tr = json.load(open(tr_path))
-            traffic = float(tr['dram_bytes_per_vis']) * n_vis + float(tr['dram_bytes_per_grid_byte']) * grid_bytes
+            if int(tr.get('n_vis', -1)) == n_vis and int(tr.get('grid_bytes', -1)) == grid_bytes:
+                traffic = float(tr['dram_bytes_read']) + float(tr['dram_bytes_write'])   # captured at this size
+            else:   # scale a capture of another size: reads by visibilities, writes by grid bytes
+                traffic = (float(tr['dram_bytes_read']) / float(tr['n_vis']) * n_vis +
+                           float(tr['dram_bytes_write']) / float(tr['grid_bytes']) * grid_bytes)
         except Exception:
             traffic = None
     roofline = {'bound': 'hbm', 'achieved': achieved, 'peak': peak, 'unit': 'GB/s', 'frac': achieved / peak,
-                'traffic': traffic, 'kernel': 'k_tiles', 'kernel_ms': t_tiles, 'binning_ms': bms,
+                'traffic': traffic, 'kernel': 'k_tiles', 'kernel_ms': t_tiles, 'prep_ms': bms,
                 'algorithmic_bytes': alg_bytes, 'peak_kind': peak_kind}
 
     # ---- end to end from pinned host buffers ----------------------------

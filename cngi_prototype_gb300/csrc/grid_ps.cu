@@ -1206,7 +1206,6 @@ extern "C" int ngg_grid_ps(const NggGridArgs *a, void *stream) {
         k_nsum<<<(a->oversampling + 1 + 127) / 128, 128, 0, s>>>(tab, tab_len, a->oversampling, nsum);
         NGG_CHECK_LAUNCH("k_nsum");
     }
-    prof_record(1, s);
 
     TileArgs ta;
     ta.vis = (const float2 *)a->vis;
@@ -1262,6 +1261,7 @@ extern "C" int ngg_grid_ps(const NggGridArgs *a, void *stream) {
         }
         ta.meta = meta;
         ta.wvp = wvp;
+        if (launch == 0) prof_record(1, s);   // phases: binning + packing | tile pass
         rc = np == 2 ? dispatch_tiles<2>(ta, n_bound, cplx, fftl, s) : dispatch_tiles<1>(ta, n_bound, cplx, fftl, s);
         if (rc != NGG_OK) return rc;
         p0 += np;

@@ -361,8 +361,10 @@ int ngg_mlp_train(float *params, float *m, float *v, const float *z, const float
 int ngg_grid_gcf_learned(const NggGcfArgs *args, const float *params, const NggMlpScale *scale, void *stream);
 
 /* Profiling: when enabled, ngg_grid_ps records CUDA events on its stream
- * around its binning phase and its tile-accumulation kernels. ngg_last_phase_ms
- * waits for the last call's events and returns the two durations (ms). */
+ * around its preparation phase (binning and the packing pass over the
+ * visibilities) and its tile pass (the zeroing of split tiles and the tile
+ * accumulation kernel). ngg_last_phase_ms waits for the last call's events
+ * and returns the two durations (ms). */
 void ngg_set_profiling(int enable);
 int ngg_last_phase_ms(double *binning_ms, double *tiles_ms);
 

@@ -36,7 +36,7 @@ __device__ __forceinline__ int pmod(int x, int m) {
 }
 
 template <bool DATA, int S>
-__global__ void __launch_bounds__(128) k_grid_gcf(const GArgs a) {
+__global__ void __launch_bounds__(128, 4) k_grid_gcf(const GArgs a) {
     constexpr int sc = S / 2;
     // per warp: S x 32 staging cells for flushes, 32 for the column transpose
     __shared__ float2 s_stage[4][S * 32];

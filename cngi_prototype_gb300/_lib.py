@@ -76,6 +76,8 @@ SIGNATURES = {
     'ngg_fft_correct_adjoint': (ctypes.c_int, [_vp, ctypes.c_int, _i64, _i64, _i64, _i64, _i64, _i64,
                                                _vp, _vp, _vp, _vp]),
     'ngg_degrid_ps': (ctypes.c_int, [ctypes.POINTER(NggDegridArgs), _vp]),
+    'ngg_rotate_uvw': (ctypes.c_int, [_vp, _vp, _i64, _i64, _vp, _vp, ctypes.c_int, ctypes.c_int, _vp, _vp, _vp]),
+    'ngg_phase_rotate': (ctypes.c_int, [_vp, _vp, _i64, _i64, _i64, _i64, _vp, ctypes.c_int, _vp, _vp]),
     'ngg_degrid_ps_noalloc': (ctypes.c_int, [ctypes.POINTER(NggDegridArgs), _vp]),
     'ngg_cell_indices': (ctypes.c_int, [_i64, _i64, _vp, _vp, _i64, _i64, ctypes.POINTER(ctypes.c_double),
                                         ctypes.c_int, ctypes.c_int, _vp, _vp, _vp]),
@@ -282,6 +284,38 @@ def fft_correct_adjoint(image, sum_weight, correction, n_uv):
                                           nm, _ptr(sw), _ptr(corr), _ptr(grid), _stream()),
            'ngg_fft_correct_adjoint')
     return grid
+
+
+def direction_rotate(vis, uvw, row_field, freq, rotmat, phase_rotation, common_tangent_reprojection=True,
+                     single_precision=True):
+    """uvw rotation and visibility phase rotation (ngg_rotate_uvw + ngg_phase_rotate).
+    vis complex64 (T,B,C,P) or None (uvw only); returns (uvw_rot (T,B,3) f64,
+    vis_rot complex64 or complex128 (T,B,C,P), or None), CUDA tensors."""
+    torch = _torch()
+    uvw_t = _dev(uvw, torch.float64, 'uvw')
+    T, B = int(uvw_t.shape[0]), int(uvw_t.shape[1])
+    rf = _dev(row_field, torch.int32, 'row_field')
+    mats = _dev(rotmat, torch.float64, 'rotmat')
+    ph = _dev(phase_rotation, torch.float64, 'phase_rotation')
+    n_field = int(mats.shape[0])
+    if rf.numel() != T:
+        raise ValueError('row_field must have one entry per time row')
+    if T * B and (int(rf.min()) < 0 or int(rf.max()) >= n_field):
+        raise ValueError('row_field index outside the field matrices')
+    uvw_rot = torch.empty((T, B, 3), dtype=torch.float64, device='cuda')
+    pd = torch.empty((T, B), dtype=torch.float64, device='cuda')
+    _check(load().ngg_rotate_uvw(_ptr(uvw_t), _ptr(rf), T, B, _ptr(mats), _ptr(ph), n_field,
+                                 1 if common_tangent_reprojection else 0, _ptr(uvw_rot), _ptr(pd), _stream()),
+           'ngg_rotate_uvw')
+    if vis is None:
+        return uvw_rot, None
+    v = _dev(vis, torch.complex64, 'vis')
+    _, _, C, P = v.shape
+    foc = _dev(np.asarray(freq, dtype=np.float64) / 299792458.0, torch.float64, 'freq_over_c')
+    out = torch.empty(v.shape, dtype=torch.complex64 if single_precision else torch.complex128, device='cuda')
+    _check(load().ngg_phase_rotate(_ptr(v), _ptr(pd), T, B, C, P, _ptr(foc), 1 if single_precision else 0,
+                                   _ptr(out), _stream()), 'ngg_phase_rotate')
+    return uvw_rot, out
 
 
 def degrid_ps(grid, uvw, weight, freq, cgk_1D, n_time_baseline_chan_pol, delta_lm, chan_mode='cube',

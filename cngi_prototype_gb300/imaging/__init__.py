@@ -1,4 +1,5 @@
 """GB300 implementation of the ngcasa.imaging hot path (same function names and parameters)."""
+from .direction_rotate import direction_rotate
 from .make_gridding_convolution_function import make_gridding_convolution_function
 from .make_image import make_image, make_psf
 from .make_image_with_gcf import make_image_with_gcf, make_psf_with_gcf

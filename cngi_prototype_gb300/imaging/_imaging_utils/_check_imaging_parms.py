@@ -78,6 +78,14 @@ def _check_imaging_weights_parms(p):
     return bool(ok)
 
 
+def _check_rotation_parms(p):
+    """_check_imaging_parms.py:96-106 of the reference."""
+    ok = _check(p, 'new_phase_center', None, list_len=2, elem_types=numbers.Number)
+    ok &= _check(p, 'common_tangent_reprojection', bool, default=True)
+    ok &= _check(p, 'single_precision', bool, default=True)
+    return bool(ok)
+
+
 def _check_norm_parms(p):
     ok = _check(p, 'norm_type', str, default='flat_sky', acceptable=['flat_noise', 'flat_sky', 'none'])
     ok &= _check(p, 'single_precision', bool, default=True)

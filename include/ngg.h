@@ -360,6 +360,28 @@ int ngg_mlp_train(float *params, float *m, float *v, const float *z, const float
  * for every tap and oversampling offset the gridder reads. */
 int ngg_grid_gcf_learned(const NggGcfArgs *args, const float *params, const NggMlpScale *scale, void *stream);
 
+/* ---- direction rotation (ngcasa/imaging/direction_rotate.py) ---------------
+ * ngg_rotate_uvw replaces apply_rotation_matrix (:189-211) and the phase-
+ * direction product of apply_phasor (:225-234): for every (time, baseline)
+ * row, uvw_rot = uvw @ rotmat[f] (row vector times the 3x3 matrix of the
+ * row's field f = row_field[time], an index into the n_field matrices) and
+ * phase_dir = uvw_rot[0:k] . phase_rotation[f][0:k], k = 2 with common
+ * tangent reprojection, else 3. uvw, uvw_rot (T,B,3) f64; rotmat (n_field,
+ * 3,3) f64 (calc_rotation_mats, :127-173, computed on the host);
+ * phase_rotation (n_field,3) f64; phase_dir (T,B) f64; row_field (T) int32. */
+int ngg_rotate_uvw(const double *uvw, const int32_t *row_field, int64_t n_time, int64_t n_baseline,
+                   const double *rotmat, const double *phase_rotation, int n_field,
+                   int common_tangent_reprojection, double *uvw_rot, double *phase_dir, void *stream);
+
+/* ngg_phase_rotate replaces the phasor of apply_phasor (:236-248):
+ * vis_rot[t,b,c,p] = vis[t,b,c,p] * exp(2 pi i phase_dir[t,b] f[c] / c).
+ * vis complex64 (T,B,C,P); freq_over_c (C) f64 = freq / 299792458;
+ * single_precision != 0: vis_rot complex64 (the reference rounds its FP64
+ * product to complex64); else complex128. */
+int ngg_phase_rotate(const void *vis, const double *phase_dir, int64_t n_time, int64_t n_baseline,
+                     int64_t n_chan, int64_t n_pol, const double *freq_over_c, int single_precision,
+                     void *vis_rot, void *stream);
+
 /* Profiling: when enabled, ngg_grid_ps records CUDA events on its stream
  * around its preparation phase (binning and the packing pass over the
  * visibilities) and its tile pass (the zeroing of split tiles and the tile

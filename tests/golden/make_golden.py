@@ -8,7 +8,8 @@ Run in a container that has the reference checkout (default
 It runs the reference's own per-chunk functions -- _standard_grid_numpy_wrap,
 _standard_grid_psf_numpy_wrap, _standard_imaging_weight_degrid_numpy_wrap,
 synthesis_imaging_cube's numpy imaging helpers, the prolate-spheroidal
-kernel builders and the GCF helpers -- through ``refshim`` on small seeded
+kernel builders, the GCF helpers and direction_rotate's rotation and phasor
+functions -- through ``refshim`` on small seeded
 synthetic inputs, and stores inputs and outputs as compressed .npz files next
 to this script. The tests read only the .npz files.
 """
@@ -216,8 +217,66 @@ def mosaic_case(R):
           'sw', sw.ravel()[:4])
 
 
+def rotate_case():
+    """direction_rotate: the reference's calc_rotation_mats, apply_rotation_matrix
+    and apply_phasor (direction_rotate.py:127-248) on a 3-field case, for both
+    common_tangent_reprojection and both single_precision settings."""
+    refshim.install()
+    import importlib
+    dr = importlib.import_module('ngcasa.imaging.direction_rotate')
+    rng = np.random.default_rng(11)
+    T, B, C, P = 10, 6, 3, 2
+    field_of_row = np.array([5, 5, 5, 5, 2, 2, 2, 9, 9, 9])
+    field_id = np.repeat(field_of_row[:, None], B, axis=1)
+    uvw = rng.uniform(-2000.0, 2000.0, (T, B, 3))
+    uvw[:, :, 2] *= 0.1
+    vis = (rng.standard_normal((T, B, C, P)) + 1j * rng.standard_normal((T, B, C, P))).astype(np.complex64)
+    freq = 100.0e9 + np.arange(C) * 0.8e9
+    new_pc = [1.2, -0.4]
+    all_ids = np.array([2, 5, 7, 9])
+    phase_dir = np.array([[1.2 + 3e-4, -0.4 - 2e-4], [1.2 - 5e-4, -0.4 + 1e-4], [0.3, 0.2], [1.2 + 1e-4, -0.4 + 6e-4]])
+
+    class Sel:
+        def __init__(self, a):
+            self.values = a
+
+        def __getitem__(self, k):
+            return Sel(self.values[k])
+
+    class PhaseDir:
+        def sel(self, field_id, d1):
+            idx = [int(np.where(all_ids == f)[0][0]) for f in field_id]
+            return Sel(phase_dir[idx])
+
+    class Obj:
+        pass
+
+    vds = Obj()
+    vds.FIELD_ID = field_id
+    fds = Obj()
+    fds.PHASE_DIR = PhaseDir()
+    out = dict(uvw=uvw, vis=vis, freq=freq, field_id=field_id, new_phase_center=np.array(new_pc),
+               field_ids=all_ids, phase_dir=phase_dir)
+    for ctr in (True, False):
+        parms = {'new_phase_center': new_pc, 'common_tangent_reprojection': ctr, 'single_precision': True}
+        rotmat, phase_rot, rot_ids = dr.calc_rotation_mats(vds, fds, parms)
+        uvw_rot = dr.apply_rotation_matrix(uvw, field_id[:, :, None], rotmat, rot_ids)
+        tag = 'ctr' if ctr else 'noctr'
+        out[f'rotmat_{tag}'] = rotmat
+        out[f'phase_rotation_{tag}'] = phase_rot
+        out[f'rot_field_id_{tag}'] = rot_ids
+        out[f'uvw_rot_{tag}'] = uvw_rot
+        for single in (True, False):
+            v = dr.apply_phasor(vis, uvw_rot[:, :, :, None], field_id[:, :, None, None], freq[None, None, :, None],
+                                phase_rot, rot_ids, ctr, single)
+            out[f'vis_rot_{tag}_{"single" if single else "double"}'] = v
+    np.savez_compressed(os.path.join(HERE, 'rotate.npz'), **out)
+
+
 if __name__ == '__main__':
     if len(sys.argv) == 1 or sys.argv[1] == 'standard':
         main()
     if len(sys.argv) == 1 or sys.argv[1] == 'mosaic':
         mosaic_case(refshim.modules())
+    if len(sys.argv) == 1 or sys.argv[1] == 'rotate':
+        rotate_case()

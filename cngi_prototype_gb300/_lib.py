@@ -76,6 +76,8 @@ SIGNATURES = {
     'ngg_fft_correct_adjoint': (ctypes.c_int, [_vp, ctypes.c_int, _i64, _i64, _i64, _i64, _i64, _i64,
                                                _vp, _vp, _vp, _vp]),
     'ngg_degrid_ps': (ctypes.c_int, [ctypes.POINTER(NggDegridArgs), _vp]),
+    'ngg_hogbom_clean': (ctypes.c_int, [_vp, _vp, _vp, _i64, _i64, _i64, _i64, _i64, ctypes.c_double, ctypes.c_double,
+                                        ctypes.c_int, ctypes.c_int, _vp, _vp]),
     'ngg_rotate_uvw': (ctypes.c_int, [_vp, _vp, _i64, _i64, _vp, _vp, ctypes.c_int, ctypes.c_int, _vp, _vp, _vp]),
     'ngg_phase_rotate': (ctypes.c_int, [_vp, _vp, _i64, _i64, _i64, _i64, _vp, ctypes.c_int, _vp, _vp]),
     'ngg_degrid_ps_noalloc': (ctypes.c_int, [ctypes.POINTER(NggDegridArgs), _vp]),
@@ -284,6 +286,30 @@ def fft_correct_adjoint(image, sum_weight, correction, n_uv):
                                           nm, _ptr(sw), _ptr(corr), _ptr(grid), _stream()),
            'ngg_fft_correct_adjoint')
     return grid
+
+
+def hogbom_clean(dirty, psf, gain, threshold, n_iter, scale_by_peak=True):
+    """Hogbom minor cycle on every plane (ngg_hogbom_clean). dirty (l, m, time,
+    chan, pol) and psf (l', m', time, chan, pol), float64; returns (model,
+    residual) CUDA float64 (l, m, time, chan, pol) and the subtractions per
+    plane (time, chan, pol) int32."""
+    torch = _torch()
+    d = _dev(dirty, torch.float64, 'dirty')
+    p = _dev(psf, torch.float64, 'psf')
+    nx, ny = int(d.shape[0]), int(d.shape[1])
+    px, py = int(p.shape[0]), int(p.shape[1])
+    planes = tuple(int(x) for x in d.shape[2:])
+    if tuple(int(x) for x in p.shape[2:]) != planes:
+        raise ValueError('psf and dirty image must have the same (time, chan, pol) planes')
+    n = int(np.prod(planes)) if planes else 1
+    res = d.reshape(nx, ny, n).permute(2, 0, 1).contiguous()
+    ps = p.reshape(px, py, n).permute(2, 0, 1).contiguous()
+    mdl = torch.zeros_like(res)
+    its = torch.zeros(n, dtype=torch.int32, device='cuda')
+    _check(load().ngg_hogbom_clean(_ptr(res), _ptr(ps), _ptr(mdl), n, nx, ny, px, py, float(gain), float(threshold),
+                                   int(n_iter), 1 if scale_by_peak else 0, _ptr(its), _stream()), 'ngg_hogbom_clean')
+    back = lambda t: t.permute(1, 2, 0).reshape((nx, ny) + planes)
+    return back(mdl), back(res), its.reshape(planes)
 
 
 def direction_rotate(vis, uvw, row_field, freq, rotmat, phase_rotation, common_tangent_reprojection=True,

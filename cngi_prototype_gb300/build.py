@@ -8,7 +8,7 @@ ROOT = os.path.dirname(HERE)
 CSRC = os.path.join(HERE, 'csrc')
 BUILD = os.path.join(HERE, '_build')
 LIB = os.path.join(HERE, 'libngg.so')
-SOURCES = ['grid_ps.cu', 'weights.cu', 'fft.cu', 'degrid.cu', 'gcf.cu', 'gcf_grid_lo.cu', 'gcf_grid_mid.cu', 'gcf_grid_hi.cu', 'mlp.cu', 'mlp_tc.cu', 'rotate.cu', 'ngg_core.cu']
+SOURCES = ['grid_ps.cu', 'weights.cu', 'fft.cu', 'degrid.cu', 'gcf.cu', 'gcf_grid_lo.cu', 'gcf_grid_mid.cu', 'gcf_grid_hi.cu', 'mlp.cu', 'mlp_tc.cu', 'rotate.cu', 'clean.cu', 'ngg_core.cu']
 ARCH = ['-gencode', 'arch=compute_103a,code=sm_103a']
 
 

@@ -382,6 +382,23 @@ int ngg_phase_rotate(const void *vis, const double *phase_dir, int64_t n_time, i
                      int64_t n_chan, int64_t n_pol, const double *freq_over_c, int single_precision,
                      void *vis_rot, void *stream);
 
+/* ---- Hogbom CLEAN minor cycle ------------------------------------------------
+ * Replaces _clean_jit with _abs_image_peaks (ngcasa/deconvolution/
+ * deconvolve_point_clean.py:174-236, 303-320), one call for all planes.
+ * residual (n_planes, nx, ny) f64: the dirty planes in, the residuals out;
+ * model (n_planes, nx, ny) f64: components added in place (zero it first);
+ * psf (n_planes, px, py) f64, centre (px/2, py/2). Per plane: the peak is
+ * the first pixel in scan order of largest |residual| (> 0, never NaN);
+ * iterate while |peak| > threshold*|first peak| and fewer than n_iter
+ * subtractions: model[peak] += gain*peak; residual -= s*psf shifted to the
+ * peak over the overlap, s = gain*peak (scale_by_peak != 0, Hogbom's
+ * algorithm) or s = gain (the reference's code as written). FP64 with the
+ * reference's rounding: bit-identical results. iterations (n_planes) int32,
+ * optional: subtractions done per plane. */
+int ngg_hogbom_clean(double *residual, const double *psf, double *model, int64_t n_planes, int64_t nx,
+                     int64_t ny, int64_t px, int64_t py, double gain, double threshold, int n_iter,
+                     int scale_by_peak, int32_t *iterations, void *stream);
+
 /* Profiling: when enabled, ngg_grid_ps records CUDA events on its stream
  * around its preparation phase (binning and the packing pass over the
  * visibilities) and its tile pass (the zeroing of split tiles and the tile

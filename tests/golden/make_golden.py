@@ -9,7 +9,7 @@ It runs the reference's own per-chunk functions -- _standard_grid_numpy_wrap,
 _standard_grid_psf_numpy_wrap, _standard_imaging_weight_degrid_numpy_wrap,
 synthesis_imaging_cube's numpy imaging helpers, the prolate-spheroidal
 kernel builders, the GCF helpers and direction_rotate's rotation and phasor
-functions -- through ``refshim`` on small seeded
+functions, and the Hogbom minor cycle -- through ``refshim`` on small seeded
 synthetic inputs, and stores inputs and outputs as compressed .npz files next
 to this script. The tests read only the .npz files.
 """
@@ -273,6 +273,43 @@ def rotate_case():
     np.savez_compressed(os.path.join(HERE, 'rotate.npz'), **out)
 
 
+def clean_case():
+    """Hogbom minor cycle: the reference's _clean_jit (deconvolve_point_clean.py
+    :174-236, as written) on dirty images and PSFs of a few point sources."""
+    refshim.install()
+    import importlib
+    import sys as _sys
+    import types as _types
+    for name in ('ngcasa.deconvolution',):
+        if name not in _sys.modules:
+            m = _types.ModuleType(name)
+            m.__path__ = [os.path.join(refshim.REF, 'ngcasa/deconvolution')]
+            _sys.modules[name] = m
+    nb = _sys.modules['numba']
+    nb.u4 = np.uint32
+    dc = importlib.import_module('ngcasa.deconvolution.deconvolve_point_clean')
+    rng = np.random.default_rng(13)
+    nx, ny, P = 40, 36, 2
+    x = np.arange(2 * nx)[:, None] - nx
+    y = np.arange(2 * ny)[None, :] - ny
+    psf1 = np.exp(-(x ** 2 + y ** 2) / 8.0) * np.cos(0.3 * x) + 0.02 * np.cos(0.9 * y)
+    psf = np.stack([psf1, psf1 * 0.9 + 0.1 * np.exp(-(x ** 2 + y ** 2) / 3.0)], axis=-1)[:, :, None, None, :]
+    dirty = np.zeros((nx, ny, 1, 1, P))
+    for p in range(P):
+        for _ in range(4):
+            px, py, a = rng.integers(3, nx - 3), rng.integers(3, ny - 3), rng.uniform(0.5, 2.0)
+            dirty[:, :, 0, 0, p] += a * psf[nx - px:2 * nx - px, ny - py:2 * ny - py, 0, 0, p]
+    dirty += 0.01 * rng.standard_normal(dirty.shape)
+    out = dict(dirty=dirty, psf=psf)
+    for gain, thr, niter in ((0.1, 0.05, 60), (0.3, 0.0, 25)):
+        res = dirty.copy()
+        mdl = np.zeros(res.shape)
+        dc._clean_jit(res, mdl, psf, gain, thr, niter)
+        out[f'model_g{gain}_n{niter}'] = mdl
+        out[f'residual_g{gain}_n{niter}'] = res
+    np.savez_compressed(os.path.join(HERE, 'clean.npz'), **out)
+
+
 if __name__ == '__main__':
     if len(sys.argv) == 1 or sys.argv[1] == 'standard':
         main()
@@ -280,3 +317,5 @@ if __name__ == '__main__':
         mosaic_case(refshim.modules())
     if len(sys.argv) == 1 or sys.argv[1] == 'rotate':
         rotate_case()
+    if len(sys.argv) == 1 or sys.argv[1] == 'clean':
+        clean_case()

@@ -312,6 +312,76 @@ def hogbom_clean(dirty, psf, gain, threshold, n_iter, scale_by_peak=True):
     return back(mdl), back(res), its.reshape(planes)
 
 
+def grid_ps_host(vis, uvw, weight, freq, cgk_1D, n_uv, delta_lm, out=None, on_chunk=None, chan_chunk=32,
+                 mode='data', layout='natural', support=7, oversampling=100):
+    """Cube gridding from host arrays to host grids, streamed by channel chunk.
+
+    The inputs (host, ideally pinned torch tensors) are copied to the device
+    once; chunk i is gridded (ngg_grid_ps on its channels) into one of two
+    device grid buffers while chunk i-1 is copied back on a second stream, so
+    the device-to-host copy of the grid -- the bulk of the traffic for a cube
+    -- overlaps the gridding, and device memory holds two chunks instead of
+    the whole grid. Each chunk's grid goes to out[c0:c1] (a host tensor of
+    shape (C, P, Nu, Nv)) or, with out=None, to a pinned staging buffer that
+    on_chunk(c0, c1, host_view) receives once it is complete (the buffer is
+    reused after on_chunk returns). Returns sum_weight (C, P) float64 on the host.
+    """
+    torch = _torch()
+    cur = torch.cuda.current_stream()
+    side = torch.cuda.Stream()
+    uvw_t = _dev(uvw, torch.float64, 'uvw')
+    w_t = _dev(weight, torch.float32, 'weight')
+    v_t = _dev(vis, torch.complex64, 'vis') if mode == 'data' else None
+    T, B, C, P = w_t.shape
+    freq = np.asarray(freq, dtype=np.float64)
+    nu, nv = int(n_uv[0]), int(n_uv[1])
+    gdt = torch.complex64 if (mode == 'data' or layout == 'fft') else torch.float32
+    cc = max(1, min(int(chan_chunk), C)) if C else 1
+    bufs = [torch.empty((cc, P, nu, nv), dtype=gdt, device='cuda') for _ in range(min(2, max(C, 1)))]
+    stage = None
+    if out is None:
+        stage = [torch.empty((cc, P, nu, nv), dtype=gdt, pin_memory=True) for _ in range(len(bufs))]
+    done = [None] * len(bufs)       # event: the buffer's copy back has finished
+    pending = [None] * len(bufs)    # (c0, c1) whose staged copy awaits on_chunk
+    sw_h = torch.empty((C, P), dtype=torch.float64)
+    sw_d = torch.empty((C, P), dtype=torch.float64, device='cuda')
+    for i, c0 in enumerate(range(0, C, cc)):
+        c1 = min(C, c0 + cc)
+        k = i % len(bufs)
+        if done[k] is not None:
+            cur.wait_event(done[k])
+            if pending[k] is not None and on_chunk is not None:
+                done[k].synchronize()
+                on_chunk(pending[k][0], pending[k][1], stage[k][:pending[k][1] - pending[k][0]])
+                pending[k] = None
+        vs = v_t[:, :, c0:c1].contiguous() if v_t is not None else None
+        ws = w_t[:, :, c0:c1].contiguous()
+        g = bufs[k][:c1 - c0]
+        grid_ps(vs, uvw_t, ws, freq[c0:c1], cgk_1D, (nu, nv), delta_lm, mode=mode, chan_mode='cube', layout=layout,
+                support=support, oversampling=oversampling, grid=g, sum_weight=sw_d[c0:c1])
+        ready = torch.cuda.Event()
+        ready.record(cur)
+        side.wait_event(ready)
+        with torch.cuda.stream(side):
+            if out is not None:
+                out[c0:c1].copy_(g, non_blocking=True)
+            else:
+                stage[k][:c1 - c0].copy_(g, non_blocking=True)
+                pending[k] = (c0, c1)
+            ev = torch.cuda.Event()
+            ev.record(side)
+        done[k] = ev
+        g.record_stream(side)
+    sw_h.copy_(sw_d)
+    side.synchronize()
+    if on_chunk is not None:
+        for k in range(len(bufs)):
+            if pending[k] is not None:
+                on_chunk(pending[k][0], pending[k][1], stage[k][:pending[k][1] - pending[k][0]])
+    cur.wait_stream(side)
+    return sw_h.numpy()
+
+
 def direction_rotate(vis, uvw, row_field, freq, rotmat, phase_rotation, common_tangent_reprojection=True,
                      single_precision=True):
     """uvw rotation and visibility phase rotation (ngg_rotate_uvw + ngg_phase_rotate).

@@ -8,6 +8,7 @@ import numpy as np
 from ..xds import set_var
 from ._imaging_utils._check_imaging_parms import _check_grid_parms
 from ._imaging_utils import _pipeline
+from ._imaging_utils._beam_fit import LazyBeamFit
 from ._imaging_utils._sel import _check_sel_parms, _register_group
 
 
@@ -34,7 +35,8 @@ def _make(vis_mxds, img_xds, grid_parms, vis_sel_parms, img_sel_parms, do_psf, c
     assert 'xds' in _vsp, '######### ERROR: xds must be specified in sel_parms'
     _vis = _mxds.attrs[_vsp['xds']]
     _check_sel_parms(_vis, _vsp)
-    new = {'sum_weight': 'PSF_SUM_WEIGHT', 'psf': 'PSF'} if do_psf else {'sum_weight': 'SUM_WEIGHT', 'image': 'IMAGE'}
+    new = ({'sum_weight': 'PSF_SUM_WEIGHT', 'psf': 'PSF', 'psf_fit': 'PSF_FIT'} if do_psf
+           else {'sum_weight': 'SUM_WEIGHT', 'image': 'IMAGE'})
     _check_sel_parms(_img, _isp, new_or_modified_data_variables=new, append_to_in_id=True)
     gin, gout = _vsp['data_group_in'], _isp['data_group_out']
     iw_name = gin.get('imaging_weight', gin.get('weight'))
@@ -44,6 +46,12 @@ def _make(vis_mxds, img_xds, grid_parms, vis_sel_parms, img_sel_parms, do_psf, c
     _img = _image_coords(_img, _gp, _vis, _gp['chan_mode'])
     set_var(_img, gout['sum_weight'], sw[None, :, :], ('time', 'chan', 'pol'))
     set_var(_img, gout['psf' if do_psf else 'image'], image[:, :, None, :, :], ('l', 'm', 'time', 'chan', 'pol'))
+    if do_psf and min(image.shape[0], image.shape[1]) >= 9:
+        # the Gaussian beam fit of the PSF main lobe (make_psf.py:159 calls
+        # cngi.image.fit_gaussian), evaluated when PSF_FIT is first read
+        delta = np.asarray(_gp['cell_size'], dtype=np.float64) * 3600.0 * 180.0 / np.pi
+        set_var(_img, gout['psf_fit'], LazyBeamFit(image[:, :, None, :, :], delta),
+                ('time', 'chan', 'pol', 'elps_index'))
     _register_group(_img, gout)
     return _img
 
@@ -59,9 +67,11 @@ def make_image(vis_mxds, img_xds, grid_parms, vis_sel_parms, img_sel_parms):
 
 
 def make_psf(vis_mxds, img_xds, grid_parms, vis_sel_parms, img_sel_parms):
-    """PSF (the image of the imaging weights) and PSF_SUM_WEIGHT.
+    """PSF (the image of the imaging weights), PSF_SUM_WEIGHT and PSF_FIT.
 
-    The reference also fits a Gaussian beam (cngi.image.fit_gaussian); that
-    host-side fit is not part of this library.
+    PSF_FIT (time, chan, pol, 3): major / minor FWHM (arcsec) and position
+    angle (degrees) of the elliptical Gaussian fitted to the PSF main lobe, as
+    the reference's cngi.image.fit_gaussian computes it; like the reference's
+    dask result it is evaluated on first access.
     """
     return _make(vis_mxds, img_xds, grid_parms, vis_sel_parms, img_sel_parms, True)

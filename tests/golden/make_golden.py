@@ -9,7 +9,7 @@ It runs the reference's own per-chunk functions -- _standard_grid_numpy_wrap,
 _standard_grid_psf_numpy_wrap, _standard_imaging_weight_degrid_numpy_wrap,
 synthesis_imaging_cube's numpy imaging helpers, the prolate-spheroidal
 kernel builders, the GCF helpers and direction_rotate's rotation and phasor
-functions, and the Hogbom minor cycle -- through ``refshim`` on small seeded
+functions, the Hogbom minor cycle and the PSF beam fit -- through ``refshim`` on small seeded
 synthetic inputs, and stores inputs and outputs as compressed .npz files next
 to this script. The tests read only the .npz files.
 """
@@ -310,6 +310,19 @@ def clean_case():
     np.savez_compressed(os.path.join(HERE, 'clean.npz'), **out)
 
 
+def beam_case():
+    """PSF beam fit: the reference's casa_fit (cngi/image/fit_gaussian.py) on the
+    std_cube PSF planes (the fit make_psf attaches as PSF_FIT)."""
+    refshim.install()
+    import importlib
+    fg = importlib.import_module('cngi.image.fit_gaussian')
+    d = dict(np.load(os.path.join(HERE, 'std_cube.npz')))
+    psf = d['psf'][:, :, None, :, :]                 # (l, m, time, chan, pol)
+    delta = np.array([-45.0, 45.0])                   # arcsec; l's step is negative
+    parms = fg.casa_fit(psf, np.array([9, 9]), np.array([9, 9]), 0.35, delta)
+    np.savez_compressed(os.path.join(HERE, 'beam.npz'), psf=psf, delta=delta, ellipse_parms=parms)
+
+
 if __name__ == '__main__':
     if len(sys.argv) == 1 or sys.argv[1] == 'standard':
         main()
@@ -319,3 +332,5 @@ if __name__ == '__main__':
         rotate_case()
     if len(sys.argv) == 1 or sys.argv[1] == 'clean':
         clean_case()
+    if len(sys.argv) == 1 or sys.argv[1] == 'beam':
+        beam_case()

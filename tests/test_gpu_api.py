@@ -103,3 +103,16 @@ def test_continuum_image(ngg):
                                   d['freq'], gp)
     assert img['IMAGE'].values.shape[3] == 1
     assert _err(img['IMAGE'].values[:, :, 0], ref) < 1e-5
+
+
+def test_make_psf_attaches_the_beam_fit(ngg):
+    """PSF_FIT of make_psf (evaluated on access) against the reference's fit of
+    its own PSF (tests/golden/beam.npz); the two PSFs agree to ~1e-6."""
+    from cngi_prototype_gb300 import xds
+    from cngi_prototype_gb300.imaging import make_psf
+    d = load_golden('std_cube')
+    b = load_golden('beam')
+    psf = make_psf(_mx(d), xds.Dataset(), _gp(d), {'xds': 'xds0'}, {})
+    fit = np.asarray(psf['PSF_FIT'].data)
+    assert fit.shape == b['ellipse_parms'].shape
+    assert np.allclose(fit, b['ellipse_parms'], rtol=1e-4, atol=1e-3)

@@ -98,3 +98,15 @@ def test_empty_inputs():
     g2, sw2 = cbind.grid('data', np.zeros((0, 3, 2, 2), np.complex64), np.zeros((0, 3, 3)), np.zeros((0, 3, 2, 2)),
                          np.array([1e9, 1.1e9]), cgk, 7, 100, [40, 40], [-1e-4, 1e-4])
     assert not g2.any() and not sw2.any()
+
+
+def test_beam_fit_matches_reference():
+    """PSF beam fit (make_psf's PSF_FIT) against the reference's casa_fit
+    (tests/golden/beam.npz): the same scipy spline and optimiser calls on the
+    same objective, bit-identical."""
+    from cngi_prototype_gb300.imaging._imaging_utils._beam_fit import LazyBeamFit, fit_beam
+    d = load_golden('beam')
+    assert np.array_equal(fit_beam(d['psf'], d['delta']), d['ellipse_parms'])
+    lazy = LazyBeamFit(d['psf'], d['delta'])
+    assert lazy.shape == d['ellipse_parms'].shape and 'not computed' in repr(lazy)
+    assert np.array_equal(np.asarray(lazy), d['ellipse_parms'])

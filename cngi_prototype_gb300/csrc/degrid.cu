@@ -51,8 +51,14 @@ __global__ void __launch_bounds__(256) k_degrid(const float2 *grid, const double
     __syncthreads();
     const int64_t id = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
     if (id >= T * B * C) return;
-    const int64_t row = id / C, c = id % C;
-    const int64_t base = id * P;
+    // consecutive threads follow one (channel, baseline) track in time: their
+    // 7x7 footprints overlap (a track moves less than a cell per step), so
+    // most grid reads hit L1 instead of gathering from 32 different planes
+    const int64_t c = id / (B * T);
+    const int64_t rem = id - c * (B * T);
+    const int64_t b = rem / T, t = rem - (rem / T) * T;
+    const int64_t row = t * B + b;
+    const int64_t base = (row * C + c) * P;
     const int64_t cimg = continuum ? 0 : c;
     const DChan cp = chan[c];
     const float4 us = uvs[row];

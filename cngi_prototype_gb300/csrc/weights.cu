@@ -120,11 +120,21 @@ __global__ void k_briggs(int weighting, double numer, double robust, double nois
     __shared__ double red[32];
     double s = 0.0;
     if (weighting == NGG_WEIGHTING_BRIGGS) {
+        // sum of W^2 in FP32 pairs (GB300's FP64 rate made the FP64 loop the
+        // bound): x*x = p + e exactly (FMA), accumulated by two-sum into
+        // (hi, lo): ~48-bit sums at FP32 issue rate, then FP64 across threads
         const float *pl = density + c * nuv;
+        float hi = 0.f, lo = 0.f;
         for (int64_t i = threadIdx.x; i < nuv; i += blockDim.x) {
-            const double x = (double)pl[i];
-            s += x * x;
+            const float x = pl[i];
+            const float p = x * x;
+            const float e = fmaf(x, x, -p);
+            const float t = hi + p;
+            const float bp = t - hi;
+            lo += ((hi - (t - bp)) + (p - bp)) + e;
+            hi = t;
         }
+        s = (double)hi + (double)lo;
     }
     for (int o = 16; o > 0; o >>= 1) s += __shfl_xor_sync(0xffffffffu, s, o);
     if ((threadIdx.x & 31) == 0) red[threadIdx.x >> 5] = s;

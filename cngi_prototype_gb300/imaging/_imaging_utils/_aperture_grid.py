@@ -23,6 +23,7 @@ import numpy as np
 from ... import _lib
 from ..._lib import NggError
 from ._mosaic import field_indices
+from ._pipeline import _arr
 
 
 def _slopes(phase_gradient):
@@ -67,3 +68,32 @@ def _aperture_weight_grid_numpy_wrap(uvw, imaging_weight, field, cf_baseline_map
                                      weight_conv_kernel, weight_support, phase_gradient, freq_chan, grid_parms):
     return _run('weight', None, uvw, imaging_weight, field, cf_baseline_map, cf_chan_map, cf_pol_map,
                 weight_conv_kernel, weight_support, phase_gradient, freq_chan, grid_parms)
+
+
+def _graph_aperture_grid(vis_dataset, gcf_dataset, grid_parms, sel_parms):
+    """_graph_aperture_grid (_aperture_grid.py:25-143): [grid (u, v, C_img, P),
+    sum_weight (C_img, P)] of the mosaic gridder for the dataset's data group
+    with the GCF dataset's tables and maps; grid_parms['grid_weights'] selects
+    the weight grid (WEIGHT_CONV_KERNEL), grid_parms['do_psf'] the PSF grid.
+    One GPU call instead of the reference's dask graph and tree sum."""
+    gin = sel_parms['data_group_in']
+    grid_parms = dict(grid_parms)
+    grid_parms['field_id'] = gcf_dataset['field_id'].values   # as the reference (:59); oversampling from grid_parms
+    uvw = _arr(vis_dataset[gin['uvw']])
+    weight = _arr(vis_dataset[gin['imaging_weight']])
+    field = _arr(vis_dataset['FIELD_ID'])
+    maps = (gcf_dataset['CF_BASELINE_MAP'].values, gcf_dataset['CF_CHAN_MAP'].values, gcf_dataset['CF_POL_MAP'].values)
+    support = gcf_dataset['SUPPORT'].values
+    phase_gradient = gcf_dataset['PHASE_GRADIENT'].values
+    freq = vis_dataset.coords['chan'].values
+    if grid_parms.get('grid_weights', False):
+        grid, sw = _aperture_weight_grid_numpy_wrap(uvw, weight, field, *maps, gcf_dataset['WEIGHT_CONV_KERNEL'].values,
+                                                    support, phase_gradient, freq, grid_parms)
+    elif grid_parms.get('do_psf', False):
+        grid, sw = _aperture_psf_grid_numpy_wrap(uvw, weight, field, *maps, gcf_dataset['CONV_KERNEL'].values, support,
+                                                 phase_gradient, freq, grid_parms)
+    else:
+        grid, sw = _aperture_grid_numpy_wrap(_arr(vis_dataset[gin['data']]), uvw, weight, field, *maps,
+                                             gcf_dataset['CONV_KERNEL'].values, support, phase_gradient, freq,
+                                             grid_parms)
+    return [np.moveaxis(grid, [0, 1], [-2, -1]), np.moveaxis(sw, [0, 1], [-2, -1])]

@@ -20,6 +20,7 @@ weights are used as float32.
 import numpy as np
 
 from ... import _lib
+from ._pipeline import _arr
 
 
 def _dims(grid_parms):
@@ -63,3 +64,22 @@ def _standard_imaging_weight_degrid_numpy_wrap(grid_imaging_weight, uvw, natural
                              torch.as_tensor(dens, dtype=torch.float32, device='cuda'),
                              torch.as_tensor(f, device='cuda'), dl, grid_parms.get('chan_mode', 'cube'))
     return out.cpu().numpy().astype(np.float64)
+
+
+def _graph_standard_grid(vis_dataset, cgk_1D, grid_parms, sel_parms):
+    """_graph_standard_grid (_standard_grid.py:23-106): [grid (u, v, C_img, P),
+    sum_weight (C_img, P)] of the dataset's data group. The reference builds a
+    dask graph of per-(time, baseline, chan) chunk gridders merged by a tree
+    sum; here the whole cube is one GPU call (channel-chunked by the caller
+    when it exceeds device memory), so the result is returned computed.
+    grid_parms['do_psf'] selects the PSF (real) grid."""
+    gin = sel_parms['data_group_in']
+    uvw = vis_dataset[gin['uvw']]
+    weight = vis_dataset[gin['imaging_weight']]
+    freq = vis_dataset.coords['chan'].values
+    if grid_parms.get('do_psf', False):
+        grid, sw = _standard_grid_psf_numpy_wrap(_arr(uvw), _arr(weight), freq, cgk_1D, grid_parms)
+    else:
+        grid, sw = _standard_grid_numpy_wrap(_arr(vis_dataset[gin['data']]), _arr(uvw), _arr(weight), freq, cgk_1D,
+                                             grid_parms)
+    return [np.moveaxis(grid, [0, 1], [-2, -1]), np.moveaxis(sw, [0, 1], [-2, -1])]

@@ -196,3 +196,26 @@ def test_edge_cases(ngg):
     # bad arguments raise
     with pytest.raises(ngg.NggError):
         ngg.grid_ps(vis, uvw, w, freq, cgk, [64, 70], dl, support=5)
+
+
+def test_graph_standard_grid_matches_reference(ngg):
+    """_graph_standard_grid (reference name and arguments): dataset in,
+    [grid (u, v, C, P), sum_weight (C, P)] out, equal to the golden grids."""
+    from cngi_prototype_gb300 import xds
+    from cngi_prototype_gb300.imaging._imaging_utils import _gridding_convolutional_kernels as G
+    from cngi_prototype_gb300.imaging._imaging_utils._check_imaging_parms import _check_grid_parms
+    from cngi_prototype_gb300.imaging._imaging_utils._standard_grid import _graph_standard_grid
+    d = load_golden('std_cube')
+    gp = {'image_size': [int(x) for x in d['image_size']], 'cell_size': [float(x) for x in d['cell_arcsec']]}
+    _check_grid_parms(gp)
+    gp.update({'oversampling': 100, 'support': 7, 'complex_grid': True})
+    vds = xds.vis_dataset(d['uvw'], d['vis'], d['weight'], d['freq'])
+    vds['IMAGING_WEIGHT'] = (('time', 'baseline', 'chan', 'pol'), d['weight'])
+    sel = {'data_group_in': {'data': 'DATA', 'uvw': 'UVW', 'imaging_weight': 'IMAGING_WEIGHT'}}
+    cgk = G._create_prolate_spheroidal_kernel_1D(100, 7)
+    for flags, key, swkey in (({'do_psf': False}, 'grid', 'sum_weight'), ({'do_psf': True}, 'psf_grid', 'psf_sum_weight')):
+        g, sw = _graph_standard_grid(vds, cgk, {**gp, **flags}, sel)
+        ref = np.moveaxis(d[key], [0, 1], [-2, -1])
+        assert g.shape == ref.shape
+        assert np.abs(g - ref).max() <= 1e-5 * np.abs(ref).max()
+        assert np.allclose(sw, d[swkey], rtol=1e-6)

@@ -298,3 +298,27 @@ def test_aperture_seam_functions_match_reference(ngg, gold):
     g, sw = A._aperture_weight_grid_numpy_wrap(*common, d['weight_conv_kernel'], d['support'], d['phase_gradient'],
                                                d['freq'], gp)
     assert _peak_err(g, d['weight_grid']) < 2e-6 and np.allclose(sw, d['weight_sum_weight'], rtol=1e-6)
+
+
+def test_graph_aperture_grid_matches_reference(ngg, gold):
+    """_graph_aperture_grid (reference name and arguments): datasets in,
+    [grid (u, v, C, P), sum_weight] out, equal to the golden grids."""
+    from cngi_prototype_gb300 import xds
+    from cngi_prototype_gb300.imaging._imaging_utils._aperture_grid import _graph_aperture_grid
+    d = gold
+    gp = _gp(d)
+    gp.update({'oversampling': d['oversampling'], 'field_id': np.arange(2), 'complex_grid': True})
+    vds = xds.vis_dataset(d['uvw'], d['vis'], d['imaging_weight'], d['freq'], field_id=d['field'])
+    vds['IMAGING_WEIGHT'] = (('time', 'baseline', 'chan', 'pol'), d['imaging_weight'])
+    gcf = xds.Dataset({'CF_BASELINE_MAP': (('baseline',), d['cf_baseline_map']),
+                       'CF_CHAN_MAP': (('chan',), d['cf_chan_map']), 'CF_POL_MAP': (('pol',), d['cf_pol_map']),
+                       'CONV_KERNEL': (('a', 'b', 'c', 'x', 'y'), d['conv_kernel']),
+                       'WEIGHT_CONV_KERNEL': (('a', 'b', 'c', 'x', 'y'), d['weight_conv_kernel']),
+                       'SUPPORT': (('a', 'b', 'c', 'i'), d['support']),
+                       'PHASE_GRADIENT': (('f', 'x', 'y'), d['phase_gradient'])},
+                      coords={'field_id': ('field', np.arange(2))})
+    sel = {'data_group_in': {'data': 'DATA', 'uvw': 'UVW', 'imaging_weight': 'IMAGING_WEIGHT'}}
+    for flags, key in (({}, 'grid'), ({'do_psf': True}, 'psf_grid'), ({'grid_weights': True}, 'weight_grid')):
+        g, sw = _graph_aperture_grid(vds, gcf, {**gp, **flags}, sel)
+        assert g.shape == np.moveaxis(d[key], [0, 1], [-2, -1]).shape
+        assert _peak_err(np.moveaxis(g, [-2, -1], [0, 1]), d[key]) < 2e-6

@@ -81,6 +81,7 @@ SIGNATURES = {
     'ngg_rotate_uvw': (ctypes.c_int, [_vp, _vp, _i64, _i64, _vp, _vp, ctypes.c_int, ctypes.c_int, _vp, _vp, _vp]),
     'ngg_phase_rotate': (ctypes.c_int, [_vp, _vp, _i64, _i64, _i64, _i64, _vp, ctypes.c_int, _vp, _vp]),
     'ngg_degrid_ps_noalloc': (ctypes.c_int, [ctypes.POINTER(NggDegridArgs), _vp]),
+    'ngg_predict_ps': (ctypes.c_int, [ctypes.POINTER(NggDegridArgs), _vp]),
     'ngg_cell_indices': (ctypes.c_int, [_i64, _i64, _vp, _vp, _i64, _i64, ctypes.POINTER(ctypes.c_double),
                                         ctypes.c_int, ctypes.c_int, _vp, _vp, _vp]),
     'ngg_grid_gcf': (ctypes.c_int, [ctypes.POINTER(NggGcfArgs), _vp]),
@@ -415,7 +416,9 @@ def direction_rotate(vis, uvw, row_field, freq, rotmat, phase_rotation, common_t
 
 
 def degrid_ps(grid, uvw, weight, freq, cgk_1D, n_time_baseline_chan_pol, delta_lm, chan_mode='cube',
-              layout='natural', support=7, oversampling=100, vis=None):
+              layout='natural', support=7, oversampling=100, vis=None, normalize=False):
+    """Degrid (ngg_degrid_ps, the gridder's adjoint) or, with normalize,
+    predict (ngg_predict_ps: each visibility divided by its kernel sum)."""
     torch = _torch()
     T, B, C, P = n_time_baseline_chan_pol
     uvw_t = _dev(uvw, torch.float64, 'uvw')
@@ -439,7 +442,8 @@ def degrid_ps(grid, uvw, weight, freq, cgk_1D, n_time_baseline_chan_pol, delta_l
     a.freq = _ptr(f_t).value
     a.cgk_1D = _ptr(k_t).value
     a.vis = _ptr(vis).value
-    _check(load().ngg_degrid_ps(ctypes.byref(a), _stream()), 'ngg_degrid_ps')
+    name = 'ngg_predict_ps' if normalize else 'ngg_degrid_ps'
+    _check(getattr(load(), name)(ctypes.byref(a), _stream()), name)
     return vis
 
 

@@ -41,7 +41,9 @@ __global__ void k_dsplit(const double *uvw, int64_t T, int64_t B, float4 *uvs) {
     uvs[id] = make_float4(a.hi, a.lo, c.hi, c.lo);  // time-major, as uvw
 }
 
-template <bool FFTL>
+// NORM: prediction (ngg_predict_ps) divides each visibility by its kernel
+// sum (sum_iu conv_u)(sum_iv conv_v), so a flat grid predicts itself.
+template <bool FFTL, bool NORM>
 __global__ void __launch_bounds__(256) k_degrid(const float2 *grid, const double *uvw, const float4 *uvs,
                                                 const float *weight, const DChan *chan, const double *cgk,
                                                 int tab_len, int os, int64_t T, int64_t B, int64_t C, int64_t P,
@@ -85,11 +87,15 @@ __global__ void __launch_bounds__(256) k_degrid(const float2 *grid, const double
         return;
     }
     float tu[SUP], tv[SUP];
+    float su = 0.f, sv = 0.f;
 #pragma unroll
     for (int d = 0; d < SUP; ++d) {
         tu[d] = tab[abs(os * (d - SC) + ou)];
         tv[d] = tab[abs(os * (d - SC) + ov)];
+        su += tu[d];
+        sv += tv[d];
     }
+    const float scale = NORM ? 1.0f / (su * sv) : 1.0f;
     const int64_t plane = nu * nv;
     for (int64_t p = 0; p < P; ++p) {
         const float w = weight ? weight[base + p] : 1.0f;
@@ -115,8 +121,26 @@ __global__ void __launch_bounds__(256) k_degrid(const float2 *grid, const double
             acc.x = fmaf(tu[iu], racc.x, acc.x);
             acc.y = fmaf(tu[iu], racc.y, acc.y);
         }
-        vis[base + p] = make_float2(acc.x * w, acc.y * w);
+        vis[base + p] = make_float2(acc.x * (w * scale), acc.y * (w * scale));
     }
+}
+
+template <bool FFTL, bool NORM>
+void launch_degrid_t(const NggDegridArgs *a, const float4 *uvs, const DChan *chan, int tab_len, int cont,
+                     cudaStream_t s) {
+    const int64_t n = a->n_time * a->n_baseline * a->n_chan;
+    k_degrid<FFTL, NORM><<<(unsigned)((n + 255) / 256), 256, 0, s>>>(
+        (const float2 *)a->grid, a->uvw, uvs, a->weight, chan, a->cgk_1D, tab_len, a->oversampling, a->n_time,
+        a->n_baseline, a->n_chan, a->n_pol, a->n_u, a->n_v, cont, (float2 *)a->vis);
+}
+
+void launch_degrid(const NggDegridArgs *a, const float4 *uvs, const DChan *chan, int tab_len, int cont,
+                   bool normalize, cudaStream_t s) {
+    const bool fftl = a->layout == NGG_LAYOUT_FFT;
+    if (fftl && normalize) launch_degrid_t<true, true>(a, uvs, chan, tab_len, cont, s);
+    else if (fftl) launch_degrid_t<true, false>(a, uvs, chan, tab_len, cont, s);
+    else if (normalize) launch_degrid_t<false, true>(a, uvs, chan, tab_len, cont, s);
+    else launch_degrid_t<false, false>(a, uvs, chan, tab_len, cont, s);
 }
 
 }  // namespace
@@ -124,7 +148,9 @@ __global__ void __launch_bounds__(256) k_degrid(const float2 *grid, const double
 
 using namespace ngg;
 
-extern "C" int ngg_degrid_ps(const NggDegridArgs *a, void *stream) {
+namespace {
+// Body of ngg_degrid_ps and ngg_predict_ps (normalize: divide by the kernel sum).
+int degrid_alloc(const NggDegridArgs *a, void *stream, bool normalize) {
     clear_error();
     if (!a) return fail(NGG_ERR_INVALID, "args is NULL");
     cudaStream_t s = (cudaStream_t)stream;
@@ -147,22 +173,19 @@ extern "C" int ngg_degrid_ps(const NggDegridArgs *a, void *stream) {
     if (rc != NGG_OK) { scratch_free(chan, s); return rc; }
     k_dchan<<<(unsigned)((C + 127) / 128), 128, 0, s>>>(a->freq, (int)C, a->delta_lm[0], a->delta_lm[1], a->n_u, a->n_v, chan);
     k_dsplit<<<(unsigned)((T * B + 255) / 256), 256, 0, s>>>(a->uvw, T, B, uvs);
-    const int64_t n = T * B * C;
     const int cont = a->chan_mode == NGG_CHAN_CONTINUUM;
-    if (a->layout == NGG_LAYOUT_FFT)
-        k_degrid<true><<<(unsigned)((n + 255) / 256), 256, 0, s>>>((const float2 *)a->grid, a->uvw, uvs, a->weight, chan,
-                                                                    a->cgk_1D, tab_len, a->oversampling, T, B, C, P,
-                                                                    a->n_u, a->n_v, cont, (float2 *)a->vis);
-    else
-        k_degrid<false><<<(unsigned)((n + 255) / 256), 256, 0, s>>>((const float2 *)a->grid, a->uvw, uvs, a->weight, chan,
-                                                                     a->cgk_1D, tab_len, a->oversampling, T, B, C, P,
-                                                                     a->n_u, a->n_v, cont, (float2 *)a->vis);
+    launch_degrid(a, uvs, chan, tab_len, cont, normalize, s);
     cudaError_t e = cudaGetLastError();
     scratch_free(uvs, s);
     scratch_free(chan, s);
     if (e != cudaSuccess) return cuda_fail(e, "k_degrid");
     return NGG_OK;
 }
+}  // namespace
+
+extern "C" int ngg_degrid_ps(const NggDegridArgs *a, void *stream) { return degrid_alloc(a, stream, false); }
+
+extern "C" int ngg_predict_ps(const NggDegridArgs *a, void *stream) { return degrid_alloc(a, stream, true); }
 
 // ---------------------------------------------------------------------------
 // Degridding without any device allocation.
@@ -242,16 +265,8 @@ extern "C" int ngg_degrid_ps_noalloc(const NggDegridArgs *a, void *stream) {
     DChan *chan = reinterpret_cast<DChan *>(reinterpret_cast<unsigned char *>(base) + sizeof(float4) * kNoAllocRows);
     k_dchan<<<(unsigned)((C + 127) / 128), 128, 0, s>>>(a->freq, (int)C, a->delta_lm[0], a->delta_lm[1], a->n_u, a->n_v, chan);
     k_dsplit<<<(unsigned)((T * B + 255) / 256), 256, 0, s>>>(a->uvw, T, B, uvs);
-    const int64_t n = T * B * C;
     const int cont = a->chan_mode == NGG_CHAN_CONTINUUM;
-    if (a->layout == NGG_LAYOUT_FFT)
-        k_degrid<true><<<(unsigned)((n + 255) / 256), 256, 0, s>>>((const float2 *)a->grid, a->uvw, uvs, a->weight, chan,
-                                                                    a->cgk_1D, tab_len, a->oversampling, T, B, C, P,
-                                                                    a->n_u, a->n_v, cont, (float2 *)a->vis);
-    else
-        k_degrid<false><<<(unsigned)((n + 255) / 256), 256, 0, s>>>((const float2 *)a->grid, a->uvw, uvs, a->weight, chan,
-                                                                     a->cgk_1D, tab_len, a->oversampling, T, B, C, P,
-                                                                     a->n_u, a->n_v, cont, (float2 *)a->vis);
+    launch_degrid(a, uvs, chan, tab_len, cont, false, s);
     NGG_CHECK_LAUNCH("k_degrid (noalloc)");
     return NGG_OK;
 }

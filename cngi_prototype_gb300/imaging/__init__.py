@@ -6,3 +6,4 @@ from .make_image_with_gcf import make_image_with_gcf, make_psf_with_gcf
 from .make_imaging_weight import make_imaging_weight
 from .make_mosaic_pb import make_mosaic_pb
 from .distributed import make_image_sharded, make_imaging_weight_sharded, make_psf_sharded, shard_vis, ShardGroup
+from .predict_modelvis_image import predict_modelvis_image

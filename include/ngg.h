@@ -204,6 +204,16 @@ typedef struct NggDegridArgs {
 
 int ngg_degrid_ps(const NggDegridArgs *args, void *stream);
 
+/* ngg_predict_ps: model visibilities from a model grid (the degridding step
+ * of predict_modelvis_image, ngcasa/imaging/predict_modelvis_image.py:20-39,
+ * a stub in the reference that lists normalise, stokes_to_corr, Fourier
+ * transform and degrid). Same arguments and footprint as ngg_degrid_ps; each
+ * visibility is divided by its kernel sum (sum conv_u)(sum conv_v), so a
+ * model grid from ngg_fft_correct_adjoint with sum_weight 1 gives
+ * vis = sum_pixels I exp(-2 pi i (u l + v m)) up to the kernel's aliasing and
+ * the oversampled table's quantisation. weight NULL predicts every row. */
+int ngg_predict_ps(const NggDegridArgs *args, void *stream);
+
 /* ngg_degrid_ps_noalloc: the same result as ngg_degrid_ps, for callers that
  * must not have the library allocate device memory (e.g. a host application
  * that owns and budgets all device memory itself). No counterpart in the

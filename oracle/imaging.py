@@ -399,3 +399,62 @@ def make_image_arrays(vis_data, uvw, imaging_weight, freq_chan, grid_parms, do_p
                              g.get('chan_mode', 'cube'))
     img = uncorrected_image(grid, g['image_size'])
     return correct_image(img, sw, corr), sw
+
+
+# --------------------------------------------------------------------------
+# model visibility prediction (predict_modelvis_image.py:20-39, a stub)
+# --------------------------------------------------------------------------
+def predict_vis(model, uvw, freq_chan, grid_parms, oversampling=100, support=7):
+    """Model visibilities (T,B,C,P) complex128 of a model image (N0,N1,C_img,P).
+
+    The reference only names the steps (predict_modelvis_image.py:36-39:
+    flat-sky normalisation, stokes_to_corr, Fourier transform, degrid). This
+    restates them with the standard gridder's own geometry run backwards:
+    model / grdsf embedded at the centre of the padded grid (the crop of
+    make_image.py:119 reversed), forward FFT in ifftshift order (the adjoint
+    of make_image.py:116-117's inverse FFT times Npad^2), then per
+    visibility the 7x7 footprint of _standard_grid.py:299-357 (same cells,
+    oversampling offsets and edge rule) read back and divided by its kernel
+    sum. C_img == 1 maps every channel to plane 0 (continuum).
+    """
+    npad = np.asarray(grid_parms['image_size_padded'])
+    size = np.asarray(grid_parms['image_size'])
+    C_img, P = model.shape[2], model.shape[3]
+    T, B = uvw.shape[:2]
+    C = len(freq_chan)
+    cgk = create_prolate_spheroidal_kernel_1D(oversampling, support)
+    corr = remove_padding(create_prolate_spheroidal_correction(npad), size)
+    scale = uv_scale(freq_chan, grid_parms['cell_size'], npad)
+    centre = npad // 2
+    half = support // 2
+    st = npad // 2 - size // 2
+    out = np.zeros((T, B, C, P), dtype=np.complex128)
+    grids = {}
+    for c in range(C):
+        ci = 0 if C_img == 1 else c
+        u_pos = uvw[:, :, 0] * scale[0, c] + centre[0]
+        v_pos = uvw[:, :, 1] * scale[1, c] + centre[1]
+        ok = ~np.isnan(u_pos) & ~np.isnan(v_pos)
+        u_pos = np.where(ok, u_pos, 0.0)
+        v_pos = np.where(ok, v_pos, 0.0)
+        cu = np.trunc(u_pos + 0.5).astype(np.int64)
+        cv = np.trunc(v_pos + 0.5).astype(np.int64)
+        ou = np.floor((cu - u_pos) * oversampling + 0.5).astype(np.int64)
+        ov = np.floor((cv - v_pos) * oversampling + 0.5).astype(np.int64)
+        ok &= (cu - half >= 0) & (cu + half < npad[0]) & (cv - half >= 0) & (cv + half < npad[1])
+        tu = [cgk[np.abs(oversampling * i + ou)] for i in range(-half, half + 1)]
+        tv = [cgk[np.abs(oversampling * i + ov)] for i in range(-half, half + 1)]
+        norm = sum(tu) * sum(tv)
+        for p in range(P):
+            if (ci, p) not in grids:
+                plane = np.zeros((npad[0], npad[1]))
+                plane[st[0]:st[0] + size[0], st[1]:st[1] + size[1]] = model[:, :, ci, p] / corr
+                grids[(ci, p)] = np.fft.fftshift(np.fft.fft2(np.fft.ifftshift(plane)))
+            g = grids[(ci, p)]
+            acc = np.zeros((T, B), dtype=np.complex128)
+            for a, iu in enumerate(range(-half, half + 1)):
+                gu = np.clip(cu + iu, 0, npad[0] - 1)
+                for b, iv in enumerate(range(-half, half + 1)):
+                    acc += tu[a] * tv[b] * g[gu, np.clip(cv + iv, 0, npad[1] - 1)]
+            out[:, :, c, p] = np.where(ok, acc / norm, 0.0)
+    return out

@@ -54,6 +54,7 @@ constexpr int ROUND = 8;    // producer round length (steps)
 constexpr int SUP = 7;
 constexpr int SC = 3;
 constexpr int MAX_TAB = 4096;
+constexpr int MAX_OS = 1000;   // oversampling limit checked on the host
 constexpr unsigned NO_CELL = 0xffffffffu;   // packed record of a step that adds nothing
 
 struct ChanParms {
@@ -142,19 +143,22 @@ template <int NP, bool CPLX>
 __global__ void __launch_bounds__(256) k_pack(const PackArgs a) {
     __shared__ uint2 s_meta[32][33];
     __shared__ float4 s_wv[32][33];
-    __shared__ float s_sw[NP][32][33];
+    __shared__ float s_sw[NP][32][9];       // per channel: the 8 row-threads' partial sums
+    __shared__ float s_nsum[MAX_OS + 1];
     const int x = threadIdx.x;
     const int64_t b = blockIdx.x;
     const int k = blockIdx.y;
     const int64_t c0 = (int64_t)blockIdx.z * 32;
     const int cu_c = (int)(a.nu / 2), cv_c = (int)(a.nv / 2);
+    for (int i = threadIdx.y * 32 + x; i <= a.os; i += 256) s_nsum[i] = a.nsum[i];
+    __syncthreads();
+    float swc[NP];   // this thread's sum_weight terms over its 4 steps
+#pragma unroll
+    for (int p = 0; p < NP; ++p) swc[p] = 0.f;
     for (int y = threadIdx.y; y < 32; y += 8) {
         const int64_t c = c0 + x, t = (int64_t)k * CH + y;
         uint2 meta = make_uint2(NO_CELL, 0u);
         float4 wv = make_float4(0.f, 0.f, 0.f, 0.f);
-        float swc[NP];
-#pragma unroll
-        for (int p = 0; p < NP; ++p) swc[p] = 0.f;
         if (c < a.C && t < a.T) {
             const float4 us = a.uvs[b * a.T + t];
             if (!isnan(us.x) && !isnan(us.z)) {
@@ -196,18 +200,19 @@ __global__ void __launch_bounds__(256) k_pack(const PackArgs a) {
                     if (any) {
                         meta = make_uint2(((unsigned)cu << 16) | (unsigned)cv,
                                           (unsigned)(ou + 32768) | ((unsigned)(ov + 32768) << 16));
-                        const float norm = a.nsum[ou + a.os / 2] * a.nsum[ov + a.os / 2];
+                        const float norm = s_nsum[ou + a.os / 2] * s_nsum[ov + a.os / 2];
 #pragma unroll
-                        for (int p = 0; p < NP; ++p) swc[p] = pv[p] ? __fmul_rn(w[p], norm) : 0.f;
+                        for (int p = 0; p < NP; ++p)
+                            if (pv[p]) swc[p] = __fadd_rn(swc[p], __fmul_rn(w[p], norm));
                     }
                 }
             }
         }
         s_meta[x][y] = meta;
         s_wv[x][y] = wv;
-#pragma unroll
-        for (int p = 0; p < NP; ++p) s_sw[p][x][y] = swc[p];
     }
+#pragma unroll
+    for (int p = 0; p < NP; ++p) s_sw[p][x][threadIdx.y] = swc[p];
     __syncthreads();
     // warp w writes channels c0 + w + 8i, lane x its step x
     for (int y = threadIdx.y; y < 32; y += 8) {
@@ -216,11 +221,17 @@ __global__ void __launch_bounds__(256) k_pack(const PackArgs a) {
         const int64_t ri = ((c * a.B + b) * a.nk + k) * CH + x;
         a.meta[ri] = s_meta[y][x];
         a.wvp[ri] = s_wv[y][x];
+    }
+    // the chunk's sum_weight partial per (channel, pol): its 8 row-threads' sums in a fixed order
+    const int e = threadIdx.y * 32 + x;
+    if (e < 32 * NP) {
+        const int cl = e % 32, p = e / 32;
+        const int64_t c = c0 + cl;
+        if (c < a.C) {
+            float v = 0.f;
 #pragma unroll
-        for (int p = 0; p < NP; ++p) {
-            float v = s_sw[p][y][x];
-            for (int o = 16; o > 0; o >>= 1) v += __shfl_xor_sync(0xffffffffu, v, o);
-            if (x == 0) a.sw_part[((c * NP + p) * a.B + b) * a.nk + k] = (double)v;
+            for (int r = 0; r < 8; ++r) v = __fadd_rn(v, s_sw[p][cl][r]);
+            a.sw_part[((c * NP + p) * a.B + b) * a.nk + k] = (double)v;
         }
     }
 }

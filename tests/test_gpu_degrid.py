@@ -40,7 +40,11 @@ def test_adjoint_identity(ngg):
         dy = op.image(y)
         lhs = float(torch.sum(torch.conj(ax) * y.to(torch.complex128)).real)
         rhs = float(torch.sum(x * dy))
-        assert abs(lhs - rhs) <= 1e-5 * (abs(lhs) + abs(rhs)), (lhs, rhs)
+        # the inner products cancel (random signs), so the FP32 error is measured
+        # against the norms that bound them (Cauchy-Schwarz), not their values
+        scale = float(torch.linalg.vector_norm(ax) * torch.linalg.vector_norm(y.to(torch.complex128)) +
+                      torch.linalg.vector_norm(x) * torch.linalg.vector_norm(dy))
+        assert abs(lhs - rhs) <= 1e-6 * scale, (lhs, rhs, scale)
 
 
 def _numpy_degrid(x, uvw, w, freq, gp, sw, corr):

@@ -50,10 +50,12 @@ def parse():
     p.add_argument('--no-e2e', action='store_true')
     p.add_argument('--no-cpu', action='store_true')
     p.add_argument('--no-err', action='store_true')
-    p.add_argument('--workload', default='large_cube', choices=['large_cube', 'mosaic', 'standard_small', 'degrid'],
+    p.add_argument('--workload', default='large_cube',
+                   choices=['large_cube', 'mosaic', 'standard_small', 'degrid', 'cycle'],
                    help='large_cube (default, the headline), mosaic (aperture-projection imaging, table and '
                         'learned GCF), standard_small (the small cube through the whole API), degrid (the '
-                        'differentiable degrid/grid pair)')
+                        'differentiable degrid/grid pair), cycle (direction_rotate, Hogbom CLEAN and '
+                        'predict_modelvis_image)')
     p.add_argument('--mosaic-chans', type=int, default=16)
     p.add_argument('--mosaic-pointings', type=int, default=49)
     p.add_argument('--no-learned', action='store_true')
@@ -479,6 +481,228 @@ def run_degrid(args, rank, world, local, dist):
                'note': 'value = model visibilities per second of one forward + chi-square + backward step'})
 
 
+def _ev_ms(fn, steps, warmup):
+    """Mean ms of fn() over `steps` calls, CUDA events on the current stream
+    (the stream every libngg call in this process is launched on)."""
+    return _timed(fn, steps, warmup)
+
+
+def run_cycle(args, rank, world, local, dist):
+    """The imaging major-cycle pieces around the gridder, each device-resident:
+    * direction_rotate on the mosaic geometry (50 x 12 m antennas in a 750 m
+      disk, 49 pointings x 30 x 6 s = 1470 times, 1225 baselines, 16 channels
+      over 100-101.6 GHz, RR/LL: 57.6M vis; one field per time row, hexagonal
+      pointings at 26 arcsec): ngg_rotate_uvw + ngg_phase_rotate (complex64);
+    * Hogbom CLEAN (ngg_hogbom_clean) of the small standard cube's dirty image
+      and PSF (512^2, 32 channels x 2 pols = 64 planes), gain 0.1, 1000
+      iterations per plane;
+    * predict_modelvis_image's device part on the degrid geometry (2048^2
+      model of 500 Gaussians, 64 antennas x 992 times, 64 channels, 1 pol:
+      128M vis): ngg_fft_correct_adjoint + ngg_predict_ps.
+    value = predicted Mvis/s; each leg reports its own rate, roofline and
+    CPU baseline (the oracle's numpy restatement on one core, on a sample)."""
+    import ctypes
+    import torch
+    from cngi_prototype_gb300 import _lib, simulate, xds
+    from cngi_prototype_gb300.imaging import make_image, make_psf
+    from cngi_prototype_gb300.imaging.direction_rotate import calc_rotation_mats, _row_fields
+    from cngi_prototype_gb300.imaging._imaging_utils import _gridding_convolutional_kernels as G
+    from cngi_prototype_gb300.imaging._imaging_utils._check_imaging_parms import _check_grid_parms
+    from cngi_prototype_gb300.imaging._imaging_utils._remove_padding import _remove_padding
+    peak, peak_kind = measured_peaks()
+    L = _lib.load()
+    st = _lib._stream()
+    out = {}
+
+    # ---- direction_rotate -------------------------------------------------
+    rng = np.random.default_rng(6 + rank)
+    enu = simulate.disk_layout(50, 750.0, rng)
+    n_pt, n_int = 49, 30
+    T = n_pt * n_int
+    uvw = simulate.earth_rotation_uvw(enu, T, 6.0)
+    B = uvw.shape[1]
+    C, P = 16, 2
+    freq = 100.0e9 + (np.arange(C) + 0.5) * 0.1e9
+    ctr = (np.deg2rad(201.4), np.deg2rad(-43.0))
+    offs = simulate.hex_offsets(n_pt, np.deg2rad(26.0 / 3600))
+    ra, dec = simulate.sin_to_radec(offs[:, 0], offs[:, 1], ctr)
+    field_ds = xds.Dataset({'PHASE_DIR': (('field_id', 'd1', 'd2'), np.stack([ra, dec], -1)[:, None, :])},
+                           coords={'field_id': ('field_id', np.arange(n_pt))})
+    field_id = np.repeat(np.repeat(np.arange(n_pt), n_int)[:, None], B, axis=1)
+    rp = {'new_phase_center': ctr, 'common_tangent_reprojection': True}
+    mats, phase, fid = calc_rotation_mats(field_id, field_ds, rp)
+    rf = _row_fields(field_id, fid)
+    g = torch.Generator(device='cuda')
+    g.manual_seed(7)
+    vis = torch.complex(torch.randn((T, B, C, P), device='cuda', generator=g),
+                        torch.randn((T, B, C, P), device='cuda', generator=g))
+    d_uvw = torch.as_tensor(uvw, device='cuda')
+    d_rf = torch.as_tensor(rf, device='cuda')
+    d_mats = torch.as_tensor(mats, device='cuda')
+    d_ph = torch.as_tensor(phase, device='cuda')
+    d_foc = torch.as_tensor(freq / 299792458.0, device='cuda')
+    uvw_rot = torch.empty((T, B, 3), dtype=torch.float64, device='cuda')
+    pd = torch.empty((T, B), dtype=torch.float64, device='cuda')
+    vis_rot = torch.empty_like(vis)
+    P_ = _lib._ptr
+
+    def rot_uvw():
+        _lib._check(L.ngg_rotate_uvw(P_(d_uvw), P_(d_rf), T, B, P_(d_mats), P_(d_ph), n_pt, 1, P_(uvw_rot), P_(pd),
+                                     st), 'ngg_rotate_uvw')
+
+    def rot_vis():
+        _lib._check(L.ngg_phase_rotate(P_(vis), P_(pd), T, B, C, P, P_(d_foc), 1, P_(vis_rot), st),
+                    'ngg_phase_rotate')
+
+    ms_uvw = _ev_ms(rot_uvw, args.steps, args.warmup)
+    ms_vis = _ev_ms(rot_vis, args.steps, args.warmup)
+    n_vis = T * B * C * P
+    rot_bytes = n_vis * 16 + T * B * 8     # vis in + out (complex64), phase per row
+    cpu_rot = None
+    if rank == 0 and not args.no_cpu:
+        from oracle import rotate as OR
+        ns = 60   # time rows in the sample
+        vs = vis[:ns].cpu().numpy()
+        t0 = time.perf_counter()
+        ur = OR.rotate_uvw(uvw[:ns], field_id[:ns], mats, fid)
+        OR.apply_phasor(vs, ur, field_id[:ns], freq, phase, fid, True, True)
+        dt = time.perf_counter() - t0
+        cpu_rot = {'value': ns * B * C * P / dt / 1e6, 'unit': 'Mvis/s', 'cores': 1, 'kind': 'port',
+                   'sample': f'{ns} of {T} time rows, all baselines, channels and pols: the oracle\'s numpy '
+                             f'restatement of apply_rotation_matrix + apply_phasor'}
+    out['direction_rotate'] = {
+        'value': n_vis / ((ms_uvw + ms_vis) * 1e-3) / 1e6, 'unit': 'Mvis/s', 'ms_per_step': ms_uvw + ms_vis,
+        'ms_rotate_uvw': ms_uvw, 'ms_phase_rotate': ms_vis, 'n_vis': n_vis,
+        'roofline': {'bound': 'hbm', 'kernel': 'k_phasor', 'achieved': rot_bytes / (ms_vis * 1e-3) / 1e9,
+                     'peak': peak, 'unit': 'GB/s', 'frac': rot_bytes / (ms_vis * 1e-3) / 1e9 / peak,
+                     'algorithmic_bytes': rot_bytes, 'peak_kind': peak_kind, 'traffic': None},
+        'cpu_baseline': cpu_rot, 'gpu_launches_per_step': 2}
+    del vis, vis_rot, uvw_rot, pd
+    torch.cuda.empty_cache()
+
+    # ---- Hogbom CLEAN -------------------------------------------------------
+    obs = simulate.config_standard_small(seed=1 + rank)
+    gp = {'image_size': list(obs.image_size), 'cell_size': list(obs.cell_arcsec), 'chan_mode': 'cube',
+          'phase_center': [0.0, 0.0]}
+    mx = xds.mxds({'xds0': xds.vis_dataset(obs.uvw, obs.vis, obs.weight, obs.freq)})
+    dirty = make_image(mx, xds.Dataset(), gp, {'xds': 'xds0'}, {})['IMAGE'].values
+    psf = make_psf(mx, xds.Dataset(), gp, {'xds': 'xds0'}, {})['PSF'].values
+    nx, ny = dirty.shape[:2]
+    n_planes = int(np.prod(dirty.shape[2:]))
+    n_iter, gain = 1000, 0.1
+    res = torch.as_tensor(np.ascontiguousarray(np.moveaxis(dirty.reshape(nx, ny, -1), 2, 0)), device='cuda')
+    res0 = res.clone()
+    ps = torch.as_tensor(np.ascontiguousarray(np.moveaxis(psf.reshape(nx, ny, -1), 2, 0)), device='cuda')
+    mdl = torch.zeros_like(res)
+    its = torch.zeros(n_planes, dtype=torch.int32, device='cuda')
+
+    def clean():
+        res.copy_(res0)
+        mdl.zero_()
+        _lib._check(L.ngg_hogbom_clean(P_(res), P_(ps), P_(mdl), n_planes, nx, ny, nx, ny, gain, 0.0, n_iter, 1,
+                                       P_(its), st), 'ngg_hogbom_clean')
+
+    ms_clean = _ev_ms(clean, args.steps, args.warmup)
+    n_its = int(its.sum().item())
+    # per subtraction a plane is read to find the next peak (nx*ny*8 bytes):
+    # the least any Hogbom cycle moves; the window subtraction adds to it
+    cl_bytes = n_its * nx * ny * 8
+    cpu_cl = None
+    if rank == 0 and not args.no_cpu:
+        from oracle import clean as OC
+        k_it = 100
+        t0 = time.perf_counter()
+        OC.clean(dirty[:, :, :1, :1, :1], psf[:, :, :1, :1, :1], gain, 0.0, k_it, True)
+        dt = time.perf_counter() - t0
+        cpu_cl = {'value': k_it / dt, 'unit': 'plane-iterations/s', 'cores': 1, 'kind': 'port',
+                  'sample': f'one 512^2 plane, {k_it} iterations: the oracle\'s numpy Hogbom (FP64)'}
+    out['hogbom_clean'] = {
+        'value': n_its / (ms_clean * 1e-3), 'unit': 'plane-iterations/s', 'ms_per_step': ms_clean,
+        'planes': n_planes, 'image': [nx, ny], 'iterations': n_its, 'gain': gain,
+        'roofline': {'bound': 'hbm', 'kernel': 'k_hogbom', 'achieved': cl_bytes / (ms_clean * 1e-3) / 1e9,
+                     'peak': peak, 'unit': 'GB/s', 'frac': cl_bytes / (ms_clean * 1e-3) / 1e9 / peak,
+                     'algorithmic_bytes': cl_bytes, 'peak_kind': peak_kind, 'traffic': None,
+                     'note': 'one CTA per plane: 64 of the SMs busy'},
+        'cpu_baseline': cpu_cl, 'gpu_launches_per_step': 1}
+    del res, res0, ps, mdl
+    torch.cuda.empty_cache()
+
+    # ---- predict_modelvis_image ----------------------------------------------
+    rng = np.random.default_rng(3 + rank)
+    enu = simulate.log_spiral_layout(64, 2500.0, rng)
+    uvw = simulate.earth_rotation_uvw(enu, 992, 8.0)
+    T, B = uvw.shape[:2]
+    C, P, N = 64, 1, 2048
+    freq = 1.0e9 + (np.arange(C) + 0.5) * (0.5e9 / C)
+    gp = {'image_size': [N, N], 'cell_size': [1.0, 1.0]}
+    _check_grid_parms(gp)
+    npad = np.asarray(gp['image_size_padded'])
+    yy, xx = torch.meshgrid(torch.arange(N, device='cuda', dtype=torch.float32),
+                            torch.arange(N, device='cuda', dtype=torch.float32), indexing='ij')
+    model = torch.zeros((N, N), dtype=torch.float32, device='cuda')
+    pos = rng.uniform(0, N, (500, 2))
+    fw = rng.uniform(2, 20, 500)
+    amp = rng.uniform(0, 1, 500)
+    for k in range(500):
+        s2 = (fw[k] / 2.3548) ** 2
+        model += float(amp[k]) * torch.exp(-((xx - float(pos[k, 0])) ** 2 + (yy - float(pos[k, 1])) ** 2) / (2 * s2))
+    m = model[:, :, None, None].expand(N, N, C, P).contiguous()
+    corr = np.ascontiguousarray(_remove_padding(G._create_prolate_spheroidal_kernel(100, 7, npad)[1], gp['image_size']))
+    ones = torch.ones((C, P), dtype=torch.float64, device='cuda')
+    cgk = G._create_prolate_spheroidal_kernel_1D(100, 7)
+    d_uvw = torch.as_tensor(uvw, device='cuda')
+    d_freq = torch.as_tensor(freq, device='cuda')
+    d_cgk = torch.as_tensor(cgk, device='cuda')
+    d_corr = torch.as_tensor(corr, device='cuda')
+    grid = torch.empty((C, P, int(npad[0]), int(npad[1])), dtype=torch.complex64, device='cuda')
+    pv = torch.empty((T, B, C, P), dtype=torch.complex64, device='cuda')
+    a = _lib.NggDegridArgs()
+    a.chan_mode = _lib.CHAN_MODES['cube']
+    a.layout = _lib.LAYOUTS['fft']
+    a.support, a.oversampling = 7, 100
+    a.n_time, a.n_baseline, a.n_chan, a.n_pol = T, B, C, P
+    a.n_u, a.n_v = int(npad[0]), int(npad[1])
+    a.delta_lm[0], a.delta_lm[1] = float(gp['cell_size'][0]), float(gp['cell_size'][1])
+    a.grid, a.uvw, a.weight, a.freq = P_(grid).value, P_(d_uvw).value, None, P_(d_freq).value
+    a.cgk_1D, a.vis = P_(d_cgk).value, P_(pv).value
+
+    def fft_adj():
+        _lib._check(L.ngg_fft_correct_adjoint(P_(m), 0, C, P, int(npad[0]), int(npad[1]), N, N, P_(ones), P_(d_corr),
+                                              P_(grid), st), 'ngg_fft_correct_adjoint')
+
+    def predict():
+        _lib._check(L.ngg_predict_ps(ctypes.byref(a), st), 'ngg_predict_ps')
+
+    ms_fft = _ev_ms(fft_adj, args.steps, args.warmup)
+    ms_pred = _ev_ms(predict, args.steps, args.warmup)
+    n_vis = T * B * C * P
+    pr_bytes = n_vis * 8 + T * B * 24 + C * P * int(npad[0]) * int(npad[1]) * 8   # vis out, uvw, grid once
+    cpu_pr = None
+    if rank == 0 and not args.no_cpu:
+        from oracle import imaging as OI
+        mh = model.cpu().numpy().astype(np.float64)[:, :, None, None]
+        t0 = time.perf_counter()
+        OI.predict_vis(mh, uvw, freq[:1], gp)
+        dt = time.perf_counter() - t0
+        cpu_pr = {'value': T * B / dt / 1e6, 'unit': 'Mvis/s', 'cores': 1, 'kind': 'port',
+                  'sample': 'channel 0 (all 2.0M rows, one 2457^2 FFT): the oracle\'s numpy predict (FP64)'}
+    value = n_vis / ((ms_fft + ms_pred) * 1e-3) / 1e6
+    out['predict_modelvis_image'] = {
+        'value': value, 'unit': 'Mvis/s', 'ms_per_step': ms_fft + ms_pred, 'ms_fft_correct_adjoint': ms_fft,
+        'ms_predict_ps': ms_pred, 'n_vis': n_vis,
+        'roofline': {'bound': 'hbm', 'kernel': 'k_degrid (normalised)',
+                     'achieved': pr_bytes / (ms_pred * 1e-3) / 1e9, 'peak': peak, 'unit': 'GB/s',
+                     'frac': pr_bytes / (ms_pred * 1e-3) / 1e9 / peak, 'algorithmic_bytes': pr_bytes,
+                     'peak_kind': peak_kind, 'traffic': None},
+        'cpu_baseline': cpu_pr}
+    if rank == 0:
+        _line(args, world, 'imaging_cycle', value, ms_fft + ms_pred,
+              {'predict': '2048^2 model, 64 ants x 992 times, 64 chan, 1 pol (128M vis)',
+               'direction_rotate': '49-pointing mosaic, 57.6M vis', 'hogbom_clean': '64 planes of 512^2',
+               'parallelism': f'replica x{world}'},
+              out['predict_modelvis_image']['roofline'], cpu_pr, None, None, None, 4 * args.steps, out)
+
+
 def run_mosaic(args, rank, world, local, dist):
     """Mosaic aperture-projection imaging with the table GCF (one step =
     ngg_grid_gcf of the whole cube, inputs resident in HBM)."""
@@ -649,7 +873,8 @@ def main():
     build.build()
     _lib.load()
     if args.workload != 'large_cube':
-        {'mosaic': run_mosaic, 'standard_small': run_standard_small, 'degrid': run_degrid}[args.workload](
+        {'mosaic': run_mosaic, 'standard_small': run_standard_small, 'degrid': run_degrid,
+         'cycle': run_cycle}[args.workload](
             args, rank, world, local, dist)
         if dist:
             dist.barrier()

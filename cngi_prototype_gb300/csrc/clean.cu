@@ -15,16 +15,26 @@
 // the results match it bit for bit) that subtracts inside the window and
 // tracks each thread's (|r|, first index) maximum, then a block reduction.
 // Warp w owns rows x = w (mod 32), lanes the columns (coalesced rows); the
-// plane stays in L2 (512^2 FP64 = 2 MB).
+// plane stays in L2 (512^2 FP64 = 2 MB). GB300 runs FP64 at a small fraction
+// of FP32, so the peak search compares |value| as the unsigned integer bit
+// pattern of the sign-cleared double (for non-negative doubles the same
+// order as the values; NaN patterns map to 0, so a NaN is never a peak) and
+// only the window subtraction uses the FP64 pipe.
 #include "ngg_internal.cuh"
 
 namespace ngg {
 namespace {
 
 struct Peak {
-    double a;      // |value|, 0 when none
-    long long i;   // linear index x*ny + y, -1 when none
+    unsigned long long a;   // bits of |value| (see mag_key), 0 when none
+    long long i;            // linear index x*ny + y, -1 when none
 };
+
+// |v| as an order-preserving integer key; NaN -> 0 (never above a peak)
+__device__ __forceinline__ unsigned long long mag_key(double v) {
+    const unsigned long long k = (unsigned long long)__double_as_longlong(v) & 0x7fffffffffffffffull;
+    return k > 0x7ff0000000000000ull ? 0ull : k;
+}
 
 __device__ __forceinline__ Peak better(Peak p, Peak q) {
     if (q.i < 0) return p;
@@ -44,7 +54,7 @@ __device__ __forceinline__ Peak block_peak(Peak p, Peak *s_red) {
     if (lane == 0) s_red[warp] = p;
     __syncthreads();
     if (warp == 0) {
-        p = lane < (int)(blockDim.x >> 5) ? s_red[lane] : Peak{0.0, -1};
+        p = lane < (int)(blockDim.x >> 5) ? s_red[lane] : Peak{0ull, -1};
         for (int o = 16; o > 0; o >>= 1) {
             Peak q;
             q.a = __shfl_xor_sync(0xffffffffu, p.a, o);
@@ -71,17 +81,17 @@ __global__ void __launch_bounds__(1024) k_hogbom(double *residual, const double 
     const int64_t pcx = px / 2, pcy = py / 2;
 
     // first peak
-    Peak p{0.0, -1};
+    Peak p{0ull, -1};
     for (int64_t x = warp; x < nx; x += nw)
         for (int64_t y = lane; y < ny; y += 32) {
-            const double a = fabs(r[x * ny + y]);
+            const unsigned long long a = mag_key(r[x * ny + y]);
             if (a > p.a) p = Peak{a, x * ny + y};   // scan order within the thread: first wins
         }
     p = block_peak(p, s_red);
     int it = 0;
     if (p.i < 0) it = n_iter;   // nothing above zero: the reference's peak is 0 (or NaN) and it stops
-    const double thr = threshold * p.a;
-    while (it < n_iter && p.a > thr) {
+    const double thr = threshold * __longlong_as_double((long long)p.a);
+    while (it < n_iter && __longlong_as_double((long long)p.a) > thr) {
         const int64_t x0 = p.i / ny, y0 = p.i - (p.i / ny) * ny;
         const double peak = r[p.i];   // signed value (all threads read it before anyone writes)
         __syncthreads();
@@ -89,7 +99,7 @@ __global__ void __launch_bounds__(1024) k_hogbom(double *residual, const double 
         const double s = scale_by_peak ? __dmul_rn(gain, peak) : gain;
         const int64_t sx = max(x0 - pcx, (int64_t)0), ex = min(x0 + (px - pcx), nx);
         const int64_t sy = max(y0 - pcy, (int64_t)0), ey = min(y0 + (py - pcy), ny);
-        Peak q{0.0, -1};
+        Peak q{0ull, -1};
         for (int64_t x = warp; x < nx; x += nw) {
             const bool rowin = x >= sx && x < ex;
             for (int64_t y = lane; y < ny; y += 32) {
@@ -98,7 +108,7 @@ __global__ void __launch_bounds__(1024) k_hogbom(double *residual, const double 
                     v = __dsub_rn(v, __dmul_rn(s, ps[(pcx + x - x0) * py + (pcy + y - y0)]));
                     r[x * ny + y] = v;
                 }
-                const double a = fabs(v);
+                const unsigned long long a = mag_key(v);
                 if (a > q.a) q = Peak{a, x * ny + y};
             }
         }

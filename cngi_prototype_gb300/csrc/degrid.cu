@@ -44,7 +44,7 @@ __global__ void k_dsplit(const double *uvw, int64_t T, int64_t B, float4 *uvs) {
 // NORM: prediction (ngg_predict_ps) divides each visibility by its kernel
 // sum (sum_iu conv_u)(sum_iv conv_v), so a flat grid predicts itself.
 template <bool FFTL, bool NORM>
-__global__ void __launch_bounds__(256) k_degrid(const float2 *grid, const double *uvw, const float4 *uvs,
+__global__ void __launch_bounds__(256, 2) k_degrid(const float2 *grid, const double *uvw, const float4 *uvs,
                                                 const float *weight, const DChan *chan, const double *cgk,
                                                 int tab_len, int os, int64_t T, int64_t B, int64_t C, int64_t P,
                                                 int64_t nu, int64_t nv, int continuum, float2 *vis) {

@@ -60,24 +60,47 @@ int get_plan(int64_t nu, int64_t nv, int batch, cufftHandle *out, bool z = false
     return NGG_OK;
 }
 
+// Per-plane 1/sum_weight (0 -> 1) of a batch, staged in shared memory: the
+// epilogues multiply by reciprocals. GB300 runs FP64 at a small fraction of
+// FP32, and two FP64 divisions per pixel and plane made these kernels
+// FP64-bound; the complex64 planes (FP32 transform) are scaled in FP32 (the
+// result is within 3 FP32 ulps of the FP64 quotient of the same FP32 value,
+// below the transform's own error), the complex128 planes in FP64 with
+// reciprocals (within 2 ulps of the FP64 quotient).
+constexpr int MAX_BATCH = 64;
+__device__ __forceinline__ void stage_inv_sw(const double *sum_weight, int plane0, int nplanes, double *isw,
+                                             float *iswf) {
+    for (int q = threadIdx.x; q < nplanes; q += blockDim.x) {
+        double sw = sum_weight[plane0 + q];
+        if (sw == 0.0) sw = 1.0;
+        isw[q] = 1.0 / sw;
+        iswf[q] = (float)isw[q];
+    }
+    __syncthreads();
+}
+
 // one thread per output pixel (l, m) of one plane batch
 template <typename C2>
 __global__ void k_crop_correct(const C2 *planes, int nplanes, int plane0, int64_t nu, int64_t nv, int64_t nl,
                                int64_t nm, int64_t n_planes_total, const double *sum_weight,
                                const double *correction, double *image) {
+    __shared__ double isw[MAX_BATCH];
+    __shared__ float iswf[MAX_BATCH];
+    stage_inv_sw(sum_weight, plane0, nplanes, isw, iswf);
     const int64_t id = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
     if (id >= nl * nm) return;
     const int64_t l = id / nm, m = id % nm;
     int64_t k1 = l - nl / 2, k2 = m - nm / 2;
     if (k1 < 0) k1 += nu;
     if (k2 < 0) k2 += nv;
-    const double corr = correction[id];
-    for (int q = 0; q < nplanes; ++q) {
-        const int64_t pl = plane0 + q;
-        double sw = sum_weight[pl];
-        if (sw == 0.0) sw = 1.0;
-        const double re = (double)planes[(int64_t)q * nu * nv + k1 * nv + k2].x;
-        image[id * n_planes_total + pl] = (re / sw) / corr;
+    const C2 *src = planes + k1 * nv + k2;
+    double *dst = image + id * n_planes_total + plane0;
+    if constexpr (sizeof(C2) == 8) {
+        const float ic = 1.0f / (float)correction[id];
+        for (int q = 0; q < nplanes; ++q) dst[q] = (double)(src[(int64_t)q * nu * nv].x * (iswf[q] * ic));
+    } else {
+        const double ic = 1.0 / correction[id];
+        for (int q = 0; q < nplanes; ++q) dst[q] = src[(int64_t)q * nu * nv].x * (isw[q] * ic);
     }
 }
 // complex64 planes -> complex128 (exact)
@@ -87,24 +110,37 @@ __global__ void k_widen(const float2 *src, double2 *dst, int64_t n) {
         dst[i] = make_double2((double)v.x, (double)v.y);
     }
 }
-// adjoint of k_crop_correct: scaled image values placed into zeroed planes
+// adjoint of k_crop_correct: one thread per padded-plane cell (k1, k2) of a
+// plane batch; cells inside the image window get the scaled image value,
+// the others zero (the whole plane is written: no separate clearing pass)
 __global__ void k_embed(const void *image, int is_f64, int nplanes, int plane0, int64_t nu, int64_t nv, int64_t nl,
                         int64_t nm, int64_t n_planes_total, const double *sum_weight, const double *correction,
                         float2 *planes) {
-    const int64_t id = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
-    if (id >= nl * nm) return;
-    const int64_t l = id / nm, m = id % nm;
-    int64_t k1 = l - nl / 2, k2 = m - nm / 2;
-    if (k1 < 0) k1 += nu;
-    if (k2 < 0) k2 += nv;
-    const double corr = correction[id];
-    for (int q = 0; q < nplanes; ++q) {
-        const int64_t pl = plane0 + q;
-        double sw = sum_weight[pl];
-        if (sw == 0.0) sw = 1.0;
-        const int64_t ii = id * n_planes_total + pl;
-        const double x = is_f64 ? ((const double *)image)[ii] : (double)((const float *)image)[ii];
-        planes[(int64_t)q * nu * nv + k1 * nv + k2] = make_float2((float)((x / sw) / corr), 0.f);
+    __shared__ double isw[MAX_BATCH];
+    __shared__ float iswf[MAX_BATCH];
+    stage_inv_sw(sum_weight, plane0, nplanes, isw, iswf);
+    const int64_t cell = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (cell >= nu * nv) return;
+    const int64_t k1 = cell / nv, k2 = cell - (cell / nv) * nv;
+    // inverse of k = (x - n/2) mod N for x in [0, n)
+    int64_t l = k1 + nl / 2, m = k2 + nm / 2;
+    if (l >= nu) l -= nu;
+    if (m >= nv) m -= nv;
+    float2 *dst = planes + cell;
+    const int64_t plane = nu * nv;
+    if (l >= nl || m >= nm) {
+        for (int q = 0; q < nplanes; ++q) dst[(int64_t)q * plane] = make_float2(0.f, 0.f);
+        return;
+    }
+    const int64_t id = l * nm + m;
+    const float ic = 1.0f / (float)correction[id];
+    const int64_t ii = id * n_planes_total + plane0;
+    if (is_f64) {
+        const double *x = (const double *)image + ii;
+        for (int q = 0; q < nplanes; ++q) dst[(int64_t)q * plane] = make_float2((float)x[q] * (iswf[q] * ic), 0.f);
+    } else {
+        const float *x = (const float *)image + ii;
+        for (int q = 0; q < nplanes; ++q) dst[(int64_t)q * plane] = make_float2(x[q] * (iswf[q] * ic), 0.f);
     }
 }
 }  // namespace
@@ -202,7 +238,6 @@ extern "C" int ngg_fft_correct_adjoint(const void *image, int is_f64, int64_t n_
     if (!grid || !sum_weight || !correction || !image) return fail(NGG_ERR_INVALID, "NULL pointer");
     const int64_t n_planes = n_img * P;
     if (n_planes == 0) return NGG_OK;
-    NGG_CUDA(cudaMemsetAsync(grid, 0, sizeof(float2) * n_planes * nu * nv, s));
     const int64_t plane_bytes = nu * nv * 8;
     int64_t batch = (4ll << 30) / plane_bytes;
     if (batch < 1) batch = 1;
@@ -212,9 +247,9 @@ extern "C" int ngg_fft_correct_adjoint(const void *image, int is_f64, int64_t n_
     for (int64_t p0 = 0; p0 < n_planes; p0 += batch) {
         const int nb = (int)((n_planes - p0) < batch ? (n_planes - p0) : batch);
         float2 *base = g + p0 * nu * nv;
-        const int64_t npx = nl * nm;
-        k_embed<<<(unsigned)((npx + 255) / 256), 256, 0, s>>>(image, is_f64, nb, (int)p0, nu, nv, nl, nm, n_planes,
-                                                              sum_weight, correction, base);
+        const int64_t ncell = nu * nv;
+        k_embed<<<(unsigned)((ncell + 255) / 256), 256, 0, s>>>(image, is_f64, nb, (int)p0, nu, nv, nl, nm, n_planes,
+                                                                sum_weight, correction, base);
         NGG_CHECK_LAUNCH("k_embed");
         cufftHandle h;
         int rc = get_plan(nu, nv, nb, &h);

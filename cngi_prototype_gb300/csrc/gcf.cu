@@ -293,17 +293,30 @@ __global__ void k_real_fftshift(const double2 *work, int64_t nq, int64_t n0, int
 
 // ---- mosaic normalisation ------------------------------------------------------
 // image (l, m, plane): image / (osc(l,m) * (ps_corr(l,m) * norm(l,m,plane))),
-// osc = sinc(dl / (n_l os0)) sinc(dm / (n_m os1)); 0 where pb < pb_limit; float32 round trip
+// osc = sinc(dl / (n_l os0)) sinc(dm / (n_m os1)); 0 where pb < pb_limit; float32 round trip.
+// The sinc factors are separable: k_sinc tabulates them once per l and per m
+// (FP64 sinpi and divisions are long sequences on GB300's FP64 pipe), so an
+// element costs three products and one division, with the same values and
+// operation order as the per-element formula.
+__global__ void k_sinc(int64_t nl, int64_t nm, int os0, int os1, double *sl, double *sm) {
+    const int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (i < nl) {
+        const double x = (double)(i - nl / 2) / (double)(nl * os0);
+        sl[i] = x == 0.0 ? 1.0 : sinpi(x) / (M_PI * x);
+    } else if (i < nl + nm) {
+        const int64_t m = i - nl;
+        const double x = (double)(m - nm / 2) / (double)(nm * os1);
+        sm[m] = x == 0.0 ? 1.0 : sinpi(x) / (M_PI * x);
+    }
+}
+
 __global__ void k_mnorm(double *image, int64_t nl, int64_t nm, int64_t np_, const double *ps, const double *nimg,
-                        const double *pb, double pb_limit, int os0, int os1, int single) {
+                        const double *pb, double pb_limit, const double *sinc_l, const double *sinc_m, int single) {
     const int64_t id = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
     if (id >= nl * nm * np_) return;
     const int64_t lm = id / np_;
-    const int64_t l = lm / nm, m = lm % nm;
-    const double xl = (double)(l - nl / 2) / (double)(nl * os0), xm = (double)(m - nm / 2) / (double)(nm * os1);
-    const double sl = xl == 0.0 ? 1.0 : sinpi(xl) / (M_PI * xl);
-    const double sm = xm == 0.0 ? 1.0 : sinpi(xm) / (M_PI * xm);
-    const double osc = sl * sm;
+    const int64_t l = lm / nm, m = lm - (lm / nm) * nm;
+    const double osc = sinc_l[l] * sinc_m[m];
     double d = ps ? ps[lm] : 1.0;
     if (nimg) d = d * nimg[id];
     double v = image[id] / (osc * d);
@@ -312,10 +325,16 @@ __global__ void k_mnorm(double *image, int64_t nl, int64_t nm, int64_t np_, cons
     image[id] = v;
 }
 
-__global__ void k_centre_div(double *image, const double *cval, int64_t np_, int64_t n) {
+// centre values -> their reciprocals (in place), then one product per element
+__global__ void k_recip(double *v, int64_t n) {
+    const int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (i < n) v[i] = 1.0 / v[i];
+}
+
+__global__ void k_centre_div(double *image, const double *inv, int64_t np_, int64_t n) {
     const int64_t id = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
     if (id >= n) return;
-    image[id] = image[id] / cval[id % np_];
+    image[id] = image[id] * inv[id % np_];
 }
 
 __global__ void k_sqrt_abs(const double *w, int64_t n, double *pb) {
@@ -636,17 +655,24 @@ extern "C" int ngg_mosaic_normalize(double *image, int64_t n_l, int64_t n_m, int
     cudaStream_t s = (cudaStream_t)stream;
     const int64_t n = n_l * n_m * n_planes;
     if (n == 0) return NGG_OK;
+    ScratchList sc(s);
+    double *sinc = nullptr;
+    int rc;
+    if ((rc = sc.get((void **)&sinc, sizeof(double) * (size_t)(n_l + n_m))) != NGG_OK) return rc;
+    k_sinc<<<(unsigned)((n_l + n_m + 255) / 256), 256, 0, s>>>(n_l, n_m, oversampling[0], oversampling[1], sinc,
+                                                                sinc + n_l);
+    NGG_CHECK_LAUNCH("k_sinc");
     k_mnorm<<<(unsigned)((n + 255) / 256), 256, 0, s>>>(image, n_l, n_m, n_planes, ps_corr, norm_image, pb, pb_limit,
-                                                        oversampling[0], oversampling[1], single_precision);
+                                                        sinc, sinc + n_l, single_precision);
     NGG_CHECK_LAUNCH("k_mnorm");
     if (centre) {
         // the centre pixels of every plane are copied out first (they are divided too)
-        ScratchList sc(s);
         double *cval = nullptr;
-        int rc;
         if ((rc = sc.get((void **)&cval, sizeof(double) * n_planes)) != NGG_OK) return rc;
         NGG_CUDA(cudaMemcpyAsync(cval, image + (centre[0] * n_m + centre[1]) * n_planes, sizeof(double) * n_planes,
                                  cudaMemcpyDeviceToDevice, s));
+        k_recip<<<(unsigned)((n_planes + 255) / 256), 256, 0, s>>>(cval, n_planes);
+        NGG_CHECK_LAUNCH("k_recip");
         k_centre_div<<<(unsigned)((n + 255) / 256), 256, 0, s>>>(image, cval, n_planes, n);
         NGG_CHECK_LAUNCH("k_centre_div");
     }

@@ -58,8 +58,10 @@ def _check_grid_parms(grid_parms):
     ok &= _check(grid_parms, 'fft_padding', numbers.Number, default=1.2, rng=[1, 10])
     ok &= _check(grid_parms, 'chan_mode', str, default='cube', acceptable=['cube', 'continuum'])
     # not in the reference: precision of the inverse FFT ('double' removes the
-    # FP32 transform's ~6e-6 error floor at ~15-25x the transform time)
-    ok &= _check(grid_parms, 'fft_precision', str, default='single', acceptable=['single', 'double'])
+    # FP32 transform's error floor, up to ~6e-6 of the peak in the image
+    # corners, at ~15-25x the transform time; 'auto' takes 'double' while the
+    # padded planes of the cube hold at most 2^26 cells, 'single' above)
+    ok &= _check(grid_parms, 'fft_precision', str, default='auto', acceptable=['auto', 'single', 'double'])
     if ok:
         grid_parms['image_size'] = np.array(grid_parms['image_size']).astype(int)
         grid_parms['image_size_padded'] = (grid_parms['fft_padding'] * grid_parms['image_size']).astype(int)

@@ -36,6 +36,21 @@ def chan_chunks(n_chan, n_pol, npad, chan_mode, budget=GRID_BUDGET_BYTES):
     return [(c0, min(n_chan, c0 + k)) for c0 in range(0, n_chan, k)]
 
 
+AUTO_FFT64_CELLS = 1 << 26
+
+
+def fft_precision(grid_parms, n_img, n_pol, npad):
+    """The inverse transform's precision: grid_parms['fft_precision'], with
+    'auto' (the default) resolved to 'double' while the cube's padded planes
+    hold at most AUTO_FFT64_CELLS cells (the FP64 transform then costs a few
+    ms and removes the FP32 transform's error in the image corners, where
+    the correction image is small) and to 'single' above."""
+    p = grid_parms.get('fft_precision', 'auto')
+    if p == 'auto':
+        return 'double' if n_img * n_pol * int(npad[0]) * int(npad[1]) <= AUTO_FFT64_CELLS else 'single'
+    return p
+
+
 def image_cube(vis, uvw, imaging_weight, freq, grid_parms, do_psf, normalize=True):
     """Dirty image or PSF (N0, N1, C_img, P) float64 and sum_weight (C_img, P).
 
@@ -57,6 +72,7 @@ def image_cube(vis, uvw, imaging_weight, freq, grid_parms, do_psf, normalize=Tru
     cgk_d = _lib._dev(cgk, torch.float64, 'cgk_1D')
     corr_d = _lib._dev(corr, torch.float64, 'correction')
     n_img = 1 if chan_mode == 'continuum' else C
+    precision = fft_precision(grid_parms, n_img, P, npad)
     image = np.empty((int(image_size[0]), int(image_size[1]), n_img, P), dtype=np.float64)
     sum_weight = np.empty((n_img, P), dtype=np.float64)
     for c0, c1 in chan_chunks(C, P, npad, chan_mode):
@@ -67,8 +83,7 @@ def image_cube(vis, uvw, imaging_weight, freq, grid_parms, do_psf, normalize=Tru
             vv = _slice_chan(v, c0, c1) if (c0, c1) != (0, C) else v
         g, sw = _lib.grid_ps(vv, uvw_d, wv, freq[c0:c1], cgk_d, npad, cell, mode='psf' if do_psf else 'data',
                              chan_mode=chan_mode, layout='fft', support=SUPPORT, oversampling=OVERSAMPLING)
-        img = _lib.fft_correct(g, sw if normalize else torch.ones_like(sw), corr_d, image_size,
-                               precision=grid_parms.get('fft_precision', 'single'))
+        img = _lib.fft_correct(g, sw if normalize else torch.ones_like(sw), corr_d, image_size, precision=precision)
         del g
         if chan_mode == 'continuum':
             image[:, :, 0:1] = img.cpu().numpy()

@@ -47,11 +47,29 @@ def test_make_image_double_precision_fft(ngg, name):
     from cngi_prototype_gb300.imaging import make_image
     d = load_golden(name)
     mx = _mx(d)
-    single = make_image(mx, xds.Dataset(), _gp(d), {'xds': 'xds0'}, {})['IMAGE'].values[:, :, 0]
+    single = make_image(mx, xds.Dataset(), dict(_gp(d), fft_precision='single'), {'xds': 'xds0'},
+                        {})['IMAGE'].values[:, :, 0]
     gp = dict(_gp(d), fft_precision='double')
     double = make_image(mx, xds.Dataset(), gp, {'xds': 'xds0'}, {})['IMAGE'].values[:, :, 0]
     e1, e2 = _err(single, d['image']), _err(double, d['image'])
     assert e2 < 1e-5 and e2 <= e1 * 1.01 + 1e-9, (e1, e2)
+
+
+def test_auto_fft_precision_is_double_for_small_cubes(ngg):
+    """The default 'auto' runs the FP64 transform while the padded planes hold
+    at most 2^26 cells (here 2 x 2 planes of 76^2), the FP32 one above."""
+    from cngi_prototype_gb300 import xds
+    from cngi_prototype_gb300.imaging import make_image
+    from cngi_prototype_gb300.imaging._imaging_utils._pipeline import fft_precision
+    d = load_golden('std_cube')
+    mx = _mx(d)
+    auto = make_image(mx, xds.Dataset(), _gp(d), {'xds': 'xds0'}, {})['IMAGE'].values
+    double = make_image(mx, xds.Dataset(), dict(_gp(d), fft_precision='double'), {'xds': 'xds0'},
+                        {})['IMAGE'].values
+    assert np.abs(auto - double).max() <= 1e-6 * np.abs(double).max()   # gridding atomics vary in FP32 rounding
+    assert fft_precision({}, 256, 2, (4915, 4915)) == 'single'
+    assert fft_precision({}, 32, 2, (614, 614)) == 'double'
+    assert fft_precision({'fft_precision': 'single'}, 1, 1, (8, 8)) == 'single'
 
 
 @pytest.mark.parametrize('weighting,robust', [('briggs', 0.5), ('uniform', 0.0), ('briggs', -1.3)])

@@ -1039,8 +1039,9 @@ def main():
         d2h = grid_bytes + C * P * 8
         e2e = {'value': n_vis * world / (ems * 1e-3) / 1e6, 'unit': 'Mvis/s', 'h2d_bytes_per_step': int(h2d),
                'd2h_bytes_per_step': int(d2h), 'ms_per_step': ems,
-               'note': 'grid_ps_host: inputs from pinned host memory, channel chunks (32) gridded while the '
-                       'previous chunk streams back to pinned host memory; wall clock per call'}
+               'note': 'grid_ps_host: inputs in pinned host memory, read in place chunk by chunk by the '
+                       'packing kernel over the host link; channel chunks (32) gridded while the previous chunk '
+                       'streams back to pinned host memory; wall clock per call'}
         del vis_h, iw_h, uvw_h
 
     if rank == 0:

@@ -82,6 +82,7 @@ SIGNATURES = {
     'ngg_phase_rotate': (ctypes.c_int, [_vp, _vp, _i64, _i64, _i64, _i64, _vp, ctypes.c_int, _vp, _vp]),
     'ngg_degrid_ps_noalloc': (ctypes.c_int, [ctypes.POINTER(NggDegridArgs), _vp]),
     'ngg_predict_ps': (ctypes.c_int, [ctypes.POINTER(NggDegridArgs), _vp]),
+    'ngg_grid_ps_chunk': (ctypes.c_int, [ctypes.POINTER(NggGridArgs), _i64, _i64, _vp]),
     'ngg_cell_indices': (ctypes.c_int, [_i64, _i64, _vp, _vp, _i64, _i64, ctypes.POINTER(ctypes.c_double),
                                         ctypes.c_int, ctypes.c_int, _vp, _vp, _vp]),
     'ngg_grid_gcf': (ctypes.c_int, [ctypes.POINTER(NggGcfArgs), _vp]),
@@ -170,21 +171,43 @@ def _dl(delta_lm):
     return arr
 
 
+def _pinned_or_dev(x, dtype, name):
+    """A contiguous pinned host tensor of `dtype` as is (the kernels read it in
+    place), anything else as _dev makes it."""
+    torch = _torch()
+    if isinstance(x, torch.Tensor) and x.device.type == 'cpu' and x.is_pinned() and x.dtype == dtype \
+            and x.is_contiguous():
+        return x
+    return _dev(x, dtype, name)
+
+
 def grid_ps(vis, uvw, weight, freq, cgk_1D, n_uv, delta_lm, mode='data', chan_mode='cube',
-            layout='natural', support=7, oversampling=100, grid=None, sum_weight=None):
+            layout='natural', support=7, oversampling=100, grid=None, sum_weight=None, chan_offset=0,
+            chan_total=None):
     """Standard gridder on the GPU. Returns (grid, sum_weight) CUDA tensors.
 
     vis complex64 (T,B,C,P) (ignored for mode='psf'), uvw float64 (T,B,3),
     weight float32 (T,B,C,P), freq float64 (C), cgk_1D float64 table,
     n_uv padded grid size, delta_lm cell size in radians with [0] negated.
+    With chan_total, vis and weight are (T,B,chan_total,P) and the call grids
+    their channels [chan_offset, chan_offset + len(freq)) (ngg_grid_ps_chunk);
+    they may then be pinned host tensors, read in place.
     """
     torch = _torch()
     uvw_t = _dev(uvw, torch.float64, 'uvw')
-    w_t = _dev(weight, torch.float32, 'weight')
     f_t = _dev(freq, torch.float64, 'freq')
     k_t = _dev(cgk_1D, torch.float64, 'cgk_1D')
-    T, B, C, P = w_t.shape
-    v_t = _dev(vis, torch.complex64, 'vis') if mode == 'data' else None
+    if chan_total is None:
+        w_t = _dev(weight, torch.float32, 'weight')
+        T, B, C, P = w_t.shape
+        v_t = _dev(vis, torch.complex64, 'vis') if mode == 'data' else None
+    else:
+        w_t = _pinned_or_dev(weight, torch.float32, 'weight')
+        T, B, Ct, P = w_t.shape
+        C = int(f_t.shape[0])
+        if Ct != int(chan_total) or not (0 <= int(chan_offset) and int(chan_offset) + C <= Ct):
+            raise ValueError('chan_offset/chan_total do not match the weight array')
+        v_t = _pinned_or_dev(vis, torch.complex64, 'vis') if mode == 'data' else None
     n_img = 1 if chan_mode == 'continuum' else C
     nu, nv = int(n_uv[0]), int(n_uv[1])
     if grid is None:
@@ -208,7 +231,11 @@ def grid_ps(vis, uvw, weight, freq, cgk_1D, n_uv, delta_lm, mode='data', chan_mo
     a.cgk_1D = _ptr(k_t).value
     a.grid = _ptr(grid).value
     a.sum_weight = _ptr(sum_weight).value
-    _check(load().ngg_grid_ps(ctypes.byref(a), _stream()), 'ngg_grid_ps')
+    if chan_total is None:
+        _check(load().ngg_grid_ps(ctypes.byref(a), _stream()), 'ngg_grid_ps')
+    else:
+        _check(load().ngg_grid_ps_chunk(ctypes.byref(a), int(chan_offset), int(chan_total), _stream()),
+               'ngg_grid_ps_chunk')
     return grid, sum_weight
 
 
@@ -317,8 +344,11 @@ def grid_ps_host(vis, uvw, weight, freq, cgk_1D, n_uv, delta_lm, out=None, on_ch
                  mode='data', layout='natural', support=7, oversampling=100):
     """Cube gridding from host arrays to host grids, streamed by channel chunk.
 
-    The inputs (host, ideally pinned torch tensors) are copied to the device
-    once; chunk i is gridded (ngg_grid_ps on its channels) into one of two
+    Pinned host torch tensors (vis complex64, weight float32) are read in
+    place by the packing kernel, chunk by chunk, over the host link
+    (ngg_grid_ps_chunk), so the inputs' host-to-device traffic overlaps the
+    grid's copy back instead of preceding it; other inputs are copied to the
+    device once. Chunk i is gridded into one of two
     device grid buffers while chunk i-1 is copied back on a second stream, so
     the device-to-host copy of the grid -- the bulk of the traffic for a cube
     -- overlaps the gridding, and device memory holds two chunks instead of
@@ -331,8 +361,8 @@ def grid_ps_host(vis, uvw, weight, freq, cgk_1D, n_uv, delta_lm, out=None, on_ch
     cur = torch.cuda.current_stream()
     side = torch.cuda.Stream()
     uvw_t = _dev(uvw, torch.float64, 'uvw')
-    w_t = _dev(weight, torch.float32, 'weight')
-    v_t = _dev(vis, torch.complex64, 'vis') if mode == 'data' else None
+    w_t = _pinned_or_dev(weight, torch.float32, 'weight')
+    v_t = _pinned_or_dev(vis, torch.complex64, 'vis') if mode == 'data' else None
     T, B, C, P = w_t.shape
     freq = np.asarray(freq, dtype=np.float64)
     nu, nv = int(n_uv[0]), int(n_uv[1])
@@ -355,11 +385,10 @@ def grid_ps_host(vis, uvw, weight, freq, cgk_1D, n_uv, delta_lm, out=None, on_ch
                 done[k].synchronize()
                 on_chunk(pending[k][0], pending[k][1], stage[k][:pending[k][1] - pending[k][0]])
                 pending[k] = None
-        vs = v_t[:, :, c0:c1].contiguous() if v_t is not None else None
-        ws = w_t[:, :, c0:c1].contiguous()
         g = bufs[k][:c1 - c0]
-        grid_ps(vs, uvw_t, ws, freq[c0:c1], cgk_1D, (nu, nv), delta_lm, mode=mode, chan_mode='cube', layout=layout,
-                support=support, oversampling=oversampling, grid=g, sum_weight=sw_d[c0:c1])
+        grid_ps(v_t, uvw_t, w_t, freq[c0:c1], cgk_1D, (nu, nv), delta_lm, mode=mode, chan_mode='cube', layout=layout,
+                support=support, oversampling=oversampling, grid=g, sum_weight=sw_d[c0:c1], chan_offset=c0,
+                chan_total=C)
         ready = torch.cuda.Event()
         ready.record(cur)
         side.wait_event(ready)

@@ -128,6 +128,7 @@ struct PackArgs {
     float4 *wvp;              // [C][B][nk*CH]
     double *sw_part;          // [C][NP][B][nk] sum_weight partials
     int64_t T, B, C, P;
+    int64_t c_stride, c_off;  // vis/weight are (T,B,c_stride,P); this call's channels start at c_off
     int64_t nu, nv;
     int nk, p0, os;
 };
@@ -177,7 +178,7 @@ __global__ void __launch_bounds__(256) k_pack(const PackArgs a) {
                     ov = (int)o64;
                 }
                 if (cu - SC >= 0 && cu + SC < a.nu && cv - SC >= 0 && cv + SC < a.nv) {
-                    const int64_t base = ((t * a.B + b) * a.C + c) * a.P + a.p0;
+                    const int64_t base = ((t * a.B + b) * a.c_stride + a.c_off + c) * a.P + a.p0;
                     float w[NP];
                     bool pv[NP];
                     bool any = false;
@@ -1074,9 +1075,47 @@ extern "C" int ngg_last_phase_ms(double *binning_ms, double *tiles_ms) {
     return NGG_OK;
 }
 
+namespace {
+// The device address through which a kernel reads p: device memory as is,
+// pinned host memory through its mapping (read in place over the host link:
+// no copy), NULL as NULL. Pageable host memory is refused.
+int device_view(const void *p, const void **out, const char *what) {
+    *out = p;
+    if (!p) return NGG_OK;
+    cudaPointerAttributes at;
+    const cudaError_t e = cudaPointerGetAttributes(&at, p);
+    if (e != cudaSuccess) {
+        cudaGetLastError();
+        return fail(NGG_ERR_INVALID, std::string(what) + " is not a CUDA-visible pointer");
+    }
+    if (at.type == cudaMemoryTypeUnregistered)
+        return fail(NGG_ERR_INVALID, std::string(what) + " is pageable host memory (pass device or pinned host memory)");
+    if (at.type == cudaMemoryTypeHost) {
+        if (!at.devicePointer) return fail(NGG_ERR_INVALID, std::string(what) + ": pinned memory without a device mapping");
+        *out = at.devicePointer;
+    }
+    return NGG_OK;
+}
+
+int grid_ps_impl(const NggGridArgs *a, int64_t c_off, int64_t c_stride, void *stream);
+}  // namespace
+
 extern "C" int ngg_grid_ps(const NggGridArgs *a, void *stream) {
     clear_error();
     if (!a) return fail(NGG_ERR_INVALID, "args is NULL");
+    return grid_ps_impl(a, 0, a->n_chan, stream);
+}
+
+extern "C" int ngg_grid_ps_chunk(const NggGridArgs *a, int64_t chan_offset, int64_t n_chan_total, void *stream) {
+    clear_error();
+    if (!a) return fail(NGG_ERR_INVALID, "args is NULL");
+    if (chan_offset < 0 || a->n_chan < 0 || n_chan_total < chan_offset + a->n_chan)
+        return fail(NGG_ERR_INVALID, "channel range outside the input arrays");
+    return grid_ps_impl(a, chan_offset, n_chan_total, stream);
+}
+
+namespace {
+int grid_ps_impl(const NggGridArgs *a, int64_t c_off, int64_t c_stride, void *stream) {
     cudaStream_t s = (cudaStream_t)stream;
     if (a->mode != NGG_MODE_DATA && a->mode != NGG_MODE_PSF) return fail(NGG_ERR_INVALID, "mode");
     if (a->chan_mode != NGG_CHAN_CUBE && a->chan_mode != NGG_CHAN_CONTINUUM) return fail(NGG_ERR_INVALID, "chan_mode");
@@ -1094,6 +1133,12 @@ extern "C" int ngg_grid_ps(const NggGridArgs *a, void *stream) {
     if (tab_len > MAX_TAB) return fail(NGG_ERR_UNSUPPORTED, "kernel table too long");
 
     const int64_t T = a->n_time, B = a->n_baseline, C = a->n_chan, P = a->n_pol;
+    const void *vis_d = nullptr, *weight_d = nullptr;
+    {
+        int rc0 = device_view(a->mode == NGG_MODE_DATA ? a->vis : nullptr, &vis_d, "vis");
+        if (rc0 == NGG_OK) rc0 = device_view(a->weight, &weight_d, "weight");
+        if (rc0 != NGG_OK) return rc0;
+    }
     const int n_img = a->chan_mode == NGG_CHAN_CONTINUUM ? 1 : (int)C;
     const bool cplx = a->mode == NGG_MODE_DATA;
     const bool fftl = a->layout == NGG_LAYOUT_FFT;
@@ -1219,8 +1264,8 @@ extern "C" int ngg_grid_ps(const NggGridArgs *a, void *stream) {
     }
 
     TileArgs ta;
-    ta.vis = (const float2 *)a->vis;
-    ta.weight = a->weight;
+    ta.vis = (const float2 *)vis_d;
+    ta.weight = (const float *)weight_d;
     ta.uvw = a->uvw;
     ta.uvs = uvs;
     ta.chan = chan;
@@ -1247,8 +1292,8 @@ extern "C" int ngg_grid_ps(const NggGridArgs *a, void *stream) {
         ta.work_counter = counter + 2 * launch;
         if (n_chunks > 0) {
             PackArgs pa;
-            pa.vis = (const float2 *)a->vis;
-            pa.weight = a->weight;
+            pa.vis = (const float2 *)vis_d;
+            pa.weight = (const float *)weight_d;
             pa.uvw = a->uvw;
             pa.uvs = uvs;
             pa.chan = chan;
@@ -1257,6 +1302,7 @@ extern "C" int ngg_grid_ps(const NggGridArgs *a, void *stream) {
             pa.wvp = wvp;
             pa.sw_part = sw_part;
             pa.T = T; pa.B = B; pa.C = C; pa.P = P;
+            pa.c_stride = c_stride; pa.c_off = c_off;
             pa.nu = nu; pa.nv = nv;
             pa.nk = nk; pa.p0 = (int)p0; pa.os = a->oversampling;
             const dim3 pg((unsigned)B, (unsigned)nk, (unsigned)((C + 31) / 32)), pb(32, 8);
@@ -1281,6 +1327,7 @@ extern "C" int ngg_grid_ps(const NggGridArgs *a, void *stream) {
     prof_record(2, s);
     return NGG_OK;
 }
+}  // namespace
 
 extern "C" int ngg_cell_indices(int64_t n_rows, int64_t C, const double *uvw, const double *freq, int64_t nu,
                                 int64_t nv, const double delta_lm[2], int os, int mirror, int32_t *idx,

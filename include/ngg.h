@@ -92,6 +92,17 @@ typedef struct NggGridArgs {
 
 int ngg_grid_ps(const NggGridArgs *args, void *stream);
 
+/* ngg_grid_ps_chunk: the same gridding of channels [chan_offset,
+ * chan_offset + n_chan) of larger input arrays: args->vis and args->weight
+ * are (T,B,n_chan_total,P) (the reference's whole-cube arrays), args->freq
+ * and the outputs describe only the n_chan channels of this call (the
+ * per-chunk call of _graph_standard_grid, _standard_grid.py:62-75, without
+ * slicing the inputs). vis and weight may be device memory or pinned host
+ * memory; pinned host memory is read in place by the packing kernel over the
+ * host link (no staging copy). Pageable host memory is refused
+ * (NGG_ERR_INVALID), as it is by ngg_grid_ps. */
+int ngg_grid_ps_chunk(const NggGridArgs *args, int64_t chan_offset, int64_t n_chan_total, void *stream);
+
 /* Cell and oversampling-offset indices as every kernel above computes them
  * (the FP32-pair evaluation with FP64 fallback): for each uvw row r and
  * channel c, idx[(r*n_chan + c)*4 + {0,1,2,3}] = (cu, cv, ou, ov), with

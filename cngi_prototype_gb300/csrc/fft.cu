@@ -169,7 +169,7 @@ extern "C" int ngg_fft_correct(void *grid, int64_t n_img, int64_t P, int64_t nu,
     int64_t batch = (4ll << 30) / plane_bytes;
     if (batch < 1) batch = 1;
     if (batch > n_planes) batch = n_planes;
-    if (batch > 64) batch = 64;
+    if (batch > MAX_BATCH) batch = MAX_BATCH;   // the epilogues stage one value per plane of a batch
     float2 *g = (float2 *)grid;
     for (int64_t p0 = 0; p0 < n_planes; p0 += batch) {
         const int nb = (int)((n_planes - p0) < batch ? (n_planes - p0) : batch);
@@ -203,7 +203,7 @@ extern "C" int ngg_fft_correct_f64(const void *grid, int64_t n_img, int64_t P, i
     int64_t batch = (2ll << 30) / plane_bytes;
     if (batch < 1) batch = 1;
     if (batch > n_planes) batch = n_planes;
-    if (batch > 64) batch = 64;
+    if (batch > MAX_BATCH) batch = MAX_BATCH;   // the epilogues stage one value per plane of a batch
     ScratchList sl(s);
     double2 *work = nullptr;
     int rc = sl.get((void **)&work, (size_t)(batch * plane_bytes));
@@ -242,7 +242,7 @@ extern "C" int ngg_fft_correct_adjoint(const void *image, int is_f64, int64_t n_
     int64_t batch = (4ll << 30) / plane_bytes;
     if (batch < 1) batch = 1;
     if (batch > n_planes) batch = n_planes;
-    if (batch > 64) batch = 64;
+    if (batch > MAX_BATCH) batch = MAX_BATCH;   // the epilogues stage one value per plane of a batch
     float2 *g = (float2 *)grid;
     for (int64_t p0 = 0; p0 < n_planes; p0 += batch) {
         const int nb = (int)((n_planes - p0) < batch ? (n_planes - p0) : batch);

@@ -3,8 +3,9 @@
 
 Tolerances: uvw 1e-12 relative (the row-vector product's rounding order);
 complex64 output within 4 ulps of |vis| (the reference rounds its FP64
-product to complex64; the phasor here is FP32 after an FP64 reduction to a
-fraction of a turn, ~1e-7); complex128 output 1e-12 of |vis|.
+product to complex64; the phasor here is FP32 after a reduction of the phase
+to a fraction of a turn in FP32 pairs, or in FP64 beyond 2^22 turns, ~1e-7);
+complex128 output 1e-12 of |vis|.
 """
 import numpy as np
 import pytest
@@ -76,3 +77,33 @@ def test_api_adds_rotated_group(ngg):
     grp = ds.attrs['data_groups'][0]
     new = [g for g in grp.values() if g.get('data') == 'DATA_ROT']
     assert new and new[0]['uvw'] == 'UVW_ROT'
+
+
+@pytest.mark.parametrize('P', [1, 3, 4])
+def test_pol_counts_and_fp64_fallback_phases(ngg, P):
+    """Pol counts other than two (the per-pol path) and phases past 2^22 turns
+    (15,000 km baselines, field offsets to 0.05 rad: up to ~2e8 turns), which
+    take the FP64 reduction, against the oracle."""
+    from oracle import rotate as O
+    rng = np.random.default_rng(10 + P)
+    T, B, C = 6, 24, 3
+    uvw = rng.uniform(-1.5e7, 1.5e7, (T, B, 3))
+    uvw[:, : B // 2] *= 1e-3   # half the baselines below the threshold
+    field = np.repeat(np.array([0, 0, 1, 1, 2, 2])[:, None], B, axis=1)
+    vis = (rng.standard_normal((T, B, C, P)) + 1j * rng.standard_normal((T, B, C, P))).astype(np.complex64)
+    freq = 100e9 + np.arange(C) * 8e9
+    dirs = [(0.5 + 0.02, 0.3), (0.5, 0.3 - 0.03), (0.5 - 0.05, 0.3 + 0.01)]
+    mats, phase = O.rotation_mats(dirs, (0.5, 0.3), True)
+    ids = np.array([0, 1, 2])
+    ref_uvw = O.rotate_uvw(uvw, field, mats, ids)
+    rf = O.row_fields(field, ids).astype(np.int32)
+    pd = np.einsum('tbk,tk->tb', ref_uvw[:, :, :2], phase[rf, :2])
+    assert np.abs(pd).max() * freq.max() / 299792458.0 > 2.0 ** 22   # the fallback is exercised
+    ref = O.apply_phasor(vis, ref_uvw, field, freq, phase, ids, True, True)
+    _, v = ngg.direction_rotate(vis, uvw, rf, freq, mats, phase, True, True)
+    err = np.abs(v.cpu().numpy().astype(np.complex128) - ref) / np.abs(vis).max()
+    small = np.abs(pd) * freq.max() / 299792458.0 < 2.0 ** 22
+    assert err[small].max() < 5e-7
+    # ~2e8-turn phases: the FP64 products themselves differ by ~1e-16 relative
+    # between the oracle's and the kernel's operation order, ~1e-7 rad here
+    assert err.max() < 2e-6, err.max()

@@ -25,12 +25,13 @@ def _img(model):
     return xds.Dataset({'MODEL': (('l', 'm', 'time', 'chan', 'pol'), model)})
 
 
-@pytest.mark.parametrize('C,C_img,P,P_img', [(2, 2, 2, 2), (3, 1, 2, 1), (1, 1, 1, 1)])
-def test_predict_matches_oracle(ngg, C, C_img, P, P_img):
+@pytest.mark.parametrize('C,C_img,P,P_img,N0,N1', [(2, 2, 2, 2, 80, 72), (3, 1, 2, 1, 80, 72), (1, 1, 1, 1, 80, 72),
+                                                   (2, 2, 1, 1, 81, 73)])
+def test_predict_matches_oracle(ngg, C, C_img, P, P_img, N0, N1):
     from cngi_prototype_gb300.imaging import predict_modelvis_image
-    ds, uvw, freq, rng = _vis_ds(7 + C, 24, C, P)
-    gp = {'image_size': [80, 72], 'cell_size': [9.0, 9.0]}
-    model = rng.standard_normal((80, 72, 1, C_img, P_img))
+    ds, uvw, freq, rng = _vis_ds(7 + C + N0, 24, C, P)
+    gp = {'image_size': [N0, N1], 'cell_size': [9.0, 9.0]}
+    model = rng.standard_normal((N0, N1, 1, C_img, P_img))
     out = predict_modelvis_image(_img(model), ds, gp)
     got = out['MODEL'].values
     O.check_grid_parms(gp)

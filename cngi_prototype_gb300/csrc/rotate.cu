@@ -55,9 +55,8 @@ __global__ void k_split_pairs(const double *x, int64_t n, float2 *out) {
 }
 
 // phasor (cos, sin) of the phase pd[row] * f_over_c[c] (see the header)
-__device__ __forceinline__ void phasor_f32(const double *pd, const float2 *pdp, const double *f_over_c,
-                                           const float2 *focp, int64_t row, int64_t c, float &pc, float &ps) {
-    const float2 a = pdp[row], f = focp[c];
+__device__ __forceinline__ void phasor_f32(const double *__restrict__ pd, float2 a, const double *__restrict__ f_over_c,
+                                           float2 f, int64_t row, int64_t c, float &pc, float &ps) {
     const float p1 = __fmul_rn(a.x, f.x);
     float rh, rl;
     if (fabsf(p1) < 4194304.0f) {
@@ -84,32 +83,40 @@ __device__ __forceinline__ void phasor_f32(const double *pd, const float2 *pdp, 
 // load per thread cannot keep enough bytes in flight to saturate HBM).
 constexpr int PER = 4;
 template <bool VEC2, bool IDX32>
-__global__ void k_phasor_f32(const float2 *vis, const double *pd, const float2 *pdp, int64_t TB, int64_t C,
-                             int64_t P, const double *f_over_c, const float2 *focp, float2 *out) {
+__global__ void k_phasor_f32(const float2 *__restrict__ vis, const double *__restrict__ pd,
+                             const float2 *__restrict__ pdp, int64_t TB, int64_t C, int64_t P,
+                             const double *__restrict__ f_over_c, const float2 *__restrict__ focp,
+                             float2 *__restrict__ out) {
     const int64_t n = TB * C;
     if constexpr (VEC2) {
         const int64_t i0 = (int64_t)blockIdx.x * blockDim.x * PER + threadIdx.x;
+        // every load of the thread's PER elements is issued before any store
         float4 v[PER];
+        float2 a[PER], f[PER];
+        int64_t row[PER], c[PER];
 #pragma unroll
         for (int k = 0; k < PER; ++k) {
             const int64_t i = i0 + (int64_t)k * blockDim.x;
-            if (i < n) v[k] = reinterpret_cast<const float4 *>(vis)[i];
+            if (i < n) {
+                if (IDX32) {   // n < 2^31: 32-bit division (the 64-bit one is a long instruction sequence)
+                    const unsigned r32 = (unsigned)i / (unsigned)C;
+                    row[k] = r32;
+                    c[k] = (int64_t)((unsigned)i - r32 * (unsigned)C);
+                } else {
+                    row[k] = i / C;
+                    c[k] = i - row[k] * C;
+                }
+                v[k] = reinterpret_cast<const float4 *>(vis)[i];
+                a[k] = pdp[row[k]];
+                f[k] = focp[c[k]];
+            }
         }
 #pragma unroll
         for (int k = 0; k < PER; ++k) {
             const int64_t i = i0 + (int64_t)k * blockDim.x;
             if (i >= n) break;
-            int64_t row, c;
-            if (IDX32) {   // n < 2^31: 32-bit division (the 64-bit one is a long instruction sequence)
-                const unsigned r32 = (unsigned)i / (unsigned)C;
-                row = r32;
-                c = (int64_t)((unsigned)i - r32 * (unsigned)C);
-            } else {
-                row = i / C;
-                c = i - row * C;
-            }
             float pc, ps;
-            phasor_f32(pd, pdp, f_over_c, focp, row, c, pc, ps);
+            phasor_f32(pd, a[k], f_over_c, f[k], row[k], c[k], pc, ps);
             reinterpret_cast<float4 *>(out)[i] =
                 make_float4(fmaf(v[k].x, pc, -v[k].y * ps), fmaf(v[k].x, ps, v[k].y * pc),
                             fmaf(v[k].z, pc, -v[k].w * ps), fmaf(v[k].z, ps, v[k].w * pc));
@@ -119,7 +126,7 @@ __global__ void k_phasor_f32(const float2 *vis, const double *pd, const float2 *
         if (i >= n) return;
         const int64_t row = i / C, c = i - row * C;
         float pc, ps;
-        phasor_f32(pd, pdp, f_over_c, focp, row, c, pc, ps);
+        phasor_f32(pd, pdp[row], f_over_c, focp[c], row, c, pc, ps);
         const float2 *v = vis + i * P;
         float2 *o = out + i * P;
         for (int p = 0; p < P; ++p) {

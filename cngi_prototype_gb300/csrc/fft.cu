@@ -81,9 +81,9 @@ __device__ __forceinline__ void stage_inv_sw(const double *sum_weight, int plane
 
 // one thread per output pixel (l, m) of one plane batch
 template <typename C2>
-__global__ void k_crop_correct(const C2 *planes, int nplanes, int plane0, int64_t nu, int64_t nv, int64_t nl,
-                               int64_t nm, int64_t n_planes_total, const double *sum_weight,
-                               const double *correction, double *image) {
+__global__ void k_crop_correct(const C2 *__restrict__ planes, int nplanes, int plane0, int64_t nu, int64_t nv,
+                               int64_t nl, int64_t nm, int64_t n_planes_total, const double *__restrict__ sum_weight,
+                               const double *__restrict__ correction, double *__restrict__ image) {
     __shared__ double isw[MAX_BATCH];
     __shared__ float iswf[MAX_BATCH];
     stage_inv_sw(sum_weight, plane0, nplanes, isw, iswf);
@@ -93,14 +93,17 @@ __global__ void k_crop_correct(const C2 *planes, int nplanes, int plane0, int64_
     int64_t k1 = l - nl / 2, k2 = m - nm / 2;
     if (k1 < 0) k1 += nu;
     if (k2 < 0) k2 += nv;
-    const C2 *src = planes + k1 * nv + k2;
-    double *dst = image + id * n_planes_total + plane0;
+    const C2 *__restrict__ src = planes + k1 * nv + k2;
+    double *__restrict__ dst = image + id * n_planes_total + plane0;
+    const int64_t plane = nu * nv;
     if constexpr (sizeof(C2) == 8) {
         const float ic = 1.0f / (float)correction[id];
-        for (int q = 0; q < nplanes; ++q) dst[q] = (double)(src[(int64_t)q * nu * nv].x * (iswf[q] * ic));
+#pragma unroll 4
+        for (int q = 0; q < nplanes; ++q) dst[q] = (double)(src[(int64_t)q * plane].x * (iswf[q] * ic));
     } else {
         const double ic = 1.0 / correction[id];
-        for (int q = 0; q < nplanes; ++q) dst[q] = src[(int64_t)q * nu * nv].x * (isw[q] * ic);
+#pragma unroll 4
+        for (int q = 0; q < nplanes; ++q) dst[q] = src[(int64_t)q * plane].x * (isw[q] * ic);
     }
 }
 // complex64 planes -> complex128 (exact)
@@ -113,9 +116,9 @@ __global__ void k_widen(const float2 *src, double2 *dst, int64_t n) {
 // adjoint of k_crop_correct: one thread per padded-plane cell (k1, k2) of a
 // plane batch; cells inside the image window get the scaled image value,
 // the others zero (the whole plane is written: no separate clearing pass)
-__global__ void k_embed(const void *image, int is_f64, int nplanes, int plane0, int64_t nu, int64_t nv, int64_t nl,
-                        int64_t nm, int64_t n_planes_total, const double *sum_weight, const double *correction,
-                        float2 *planes) {
+__global__ void k_embed(const void *__restrict__ image, int is_f64, int nplanes, int plane0, int64_t nu, int64_t nv,
+                        int64_t nl, int64_t nm, int64_t n_planes_total, const double *__restrict__ sum_weight,
+                        const double *__restrict__ correction, float2 *__restrict__ planes) {
     __shared__ double isw[MAX_BATCH];
     __shared__ float iswf[MAX_BATCH];
     stage_inv_sw(sum_weight, plane0, nplanes, isw, iswf);
@@ -126,7 +129,7 @@ __global__ void k_embed(const void *image, int is_f64, int nplanes, int plane0, 
     int64_t l = k1 + nl / 2, m = k2 + nm / 2;
     if (l >= nu) l -= nu;
     if (m >= nv) m -= nv;
-    float2 *dst = planes + cell;
+    float2 *__restrict__ dst = planes + cell;
     const int64_t plane = nu * nv;
     if (l >= nl || m >= nm) {
         for (int q = 0; q < nplanes; ++q) dst[(int64_t)q * plane] = make_float2(0.f, 0.f);
@@ -136,10 +139,12 @@ __global__ void k_embed(const void *image, int is_f64, int nplanes, int plane0, 
     const float ic = 1.0f / (float)correction[id];
     const int64_t ii = id * n_planes_total + plane0;
     if (is_f64) {
-        const double *x = (const double *)image + ii;
+        const double *__restrict__ x = (const double *)image + ii;
+#pragma unroll 4
         for (int q = 0; q < nplanes; ++q) dst[(int64_t)q * plane] = make_float2((float)x[q] * (iswf[q] * ic), 0.f);
     } else {
-        const float *x = (const float *)image + ii;
+        const float *__restrict__ x = (const float *)image + ii;
+#pragma unroll 4
         for (int q = 0; q < nplanes; ++q) dst[(int64_t)q * plane] = make_float2(x[q] * (iswf[q] * ic), 0.f);
     }
 }

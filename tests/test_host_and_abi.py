@@ -78,3 +78,43 @@ def test_gpu_calls_fail_loudly_without_cuda():
     with pytest.raises(_lib.NggError):
         _lib.grid_ps(np.zeros((1, 1, 1, 1), np.complex64), np.zeros((1, 1, 3)), np.ones((1, 1, 1, 1), np.float32),
                      [1e9], np.ones(400), [16, 16], [-1e-4, 1e-4])
+
+
+def test_fft_precision_resolution():
+    """'auto' (the default) is FP64 up to 2^26 padded cells of the cube, FP32
+    above; explicit choices pass through; anything else is refused."""
+    from cngi_prototype_gb300.imaging._imaging_utils._check_imaging_parms import _check_grid_parms
+    from cngi_prototype_gb300.imaging._imaging_utils._pipeline import AUTO_FFT64_CELLS, fft_precision
+    gp = {'image_size': [512, 512], 'cell_size': [2.0, 2.0]}
+    assert _check_grid_parms(gp) and gp['fft_precision'] == 'auto'
+    npad = gp['image_size_padded']
+    assert fft_precision(gp, 32, 2, npad) == 'double'          # 64 planes of 614^2
+    assert fft_precision(gp, 256, 2, (4915, 4915)) == 'single'
+    side = int(np.sqrt(AUTO_FFT64_CELLS))
+    assert fft_precision({}, 1, 1, (side, side)) == 'double'
+    assert fft_precision({}, 1, 1, (side, side + 1)) == 'single'
+    for p in ('single', 'double'):
+        assert fft_precision({'fft_precision': p}, 1, 1, (8, 8)) == p
+    bad = {'image_size': [64, 64], 'cell_size': [1.0, 1.0], 'fft_precision': 'half'}
+    assert not _check_grid_parms(bad)
+
+
+def test_predict_modelvis_image_argument_checks():
+    """Model shape, channel and pol counts are checked before any device work."""
+    from cngi_prototype_gb300 import xds
+    from cngi_prototype_gb300.imaging import predict_modelvis_image
+    T, B, C, P = 3, 4, 2, 2
+    uvw = np.zeros((T, B, 3))
+    ds = xds.vis_dataset(uvw, np.zeros((T, B, C, P), np.complex64), np.ones((T, B, C, P)), [1e9, 1.1e9])
+    gp = {'image_size': [16, 16], 'cell_size': [1.0, 1.0]}
+    img = lambda m: xds.Dataset({'MODEL': (('l', 'm', 'time', 'chan', 'pol'), m)})
+    with pytest.raises(ValueError, match='image_size'):
+        predict_modelvis_image(img(np.zeros((16, 15, 1, C, P))), ds, gp)
+    with pytest.raises(ValueError, match='channels'):
+        predict_modelvis_image(img(np.zeros((16, 16, 1, 3, P))), ds, gp)
+    with pytest.raises(ValueError, match='pols'):
+        predict_modelvis_image(img(np.zeros((16, 16, 1, C, 3))), ds, gp)
+    with pytest.raises(ValueError, match='time plane'):
+        predict_modelvis_image(img(np.zeros((16, 16, 2, C, P))), ds, gp)
+    with pytest.raises(KeyError):
+        predict_modelvis_image(xds.Dataset({}), ds, gp)

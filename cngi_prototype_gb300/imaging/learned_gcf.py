@@ -17,7 +17,7 @@ footprint. The network is trained in FP32 on the GPU by libngg's own forward,
 backward and Adam kernels (ngg_mlp_train) and evaluated in BF16 on the
 tcgen05 tensor cores to synthesise one table per channel at that channel's
 exact frequency (ngg_grid_gcf_learned). The table path (ngg_grid_gcf) stays
-the fallback and the judge of the learned path's image error.
+the fallback and the yardstick for the learned path's image error.
 """
 import time
 

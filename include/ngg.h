@@ -371,7 +371,7 @@ int ngg_mlp_train(float *params, float *m, float *v, const float *z, const float
                   double *loss_history, void *stream);
 
 /* Mosaic gridding with the learned GCF in place of the table (the table path,
- * ngg_grid_gcf, stays the fallback and the judge of its error). Same
+ * ngg_grid_gcf, stays the fallback and the yardstick for its error). Same
  * arguments as ngg_grid_gcf except: conv_kernel is not read; the GCF of
  * channel c is the network evaluated at freq[c] (one table per channel, so
  * n_cf_baseline = n_cf_pol = 1 and n_cf_chan = n_chan are required and the

@@ -323,7 +323,37 @@ def beam_case():
     np.savez_compressed(os.path.join(HERE, 'beam.npz'), psf=psf, delta=delta, ellipse_parms=parms)
 
 
+def time_reference(n_time=20, n_chan=4):
+    """Time the reference's own _standard_grid_numpy_wrap (pure Python under
+    refshim's identity numba.jit) on a subsample of the small standard cube
+    (27 antennas, 351 baselines, 2 pols): the supplementary CPU figure beside
+    the C restatement. Prints microseconds per visibility (time, baseline,
+    chan, pol sample). Writes no fixture."""
+    import time
+    R = refshim.modules()
+    obs = simulate.config_standard_small(seed=1)
+    vis = np.ascontiguousarray(obs.vis[:n_time, :, :n_chan])
+    w = np.ascontiguousarray(obs.weight[:n_time, :, :n_chan]).astype(np.float64)
+    uvw = np.ascontiguousarray(obs.uvw[:n_time])
+    freq = np.asarray(obs.freq[:n_chan])
+    gp = {'image_size': [int(x) for x in obs.image_size], 'cell_size': [float(x) for x in obs.cell_arcsec],
+          'chan_mode': 'cube', 'fft_padding': 1.2}
+    assert R.cp._check_grid_parms(gp)
+    gp.update({'oversampling': 100, 'support': 7, 'complex_grid': True, 'do_psf': False})
+    cgk = R.gck._create_prolate_spheroidal_kernel_1D(100, 7)
+    t0 = time.perf_counter()
+    R.sg._standard_grid_numpy_wrap(vis, uvw, w, freq, cgk, gp)
+    dt = time.perf_counter() - t0
+    n = vis.size
+    print(f'reference _standard_grid_numpy_wrap (pure Python, identity numba.jit): {n} vis '
+          f'({n_time} times x {vis.shape[1]} baselines x {n_chan} chan x {vis.shape[3]} pols) in {dt:.2f} s = '
+          f'{dt / n * 1e6:.1f} us/vis = {n / dt / 1e6:.4f} Mvis/s, one core')
+
+
 if __name__ == '__main__':
+    if len(sys.argv) > 1 and sys.argv[1] == 'time_reference':
+        time_reference()
+        sys.exit(0)
     if len(sys.argv) == 1 or sys.argv[1] == 'standard':
         main()
     if len(sys.argv) == 1 or sys.argv[1] == 'mosaic':

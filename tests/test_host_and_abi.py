@@ -118,3 +118,24 @@ def test_predict_modelvis_image_argument_checks():
         predict_modelvis_image(img(np.zeros((16, 16, 2, C, P))), ds, gp)
     with pytest.raises(KeyError):
         predict_modelvis_image(xds.Dataset({}), ds, gp)
+
+
+def test_abi_refuses_bad_arguments_before_any_device_work():
+    """Entry points check their arguments before touching the device: with
+    no GPU present they still return NGG_ERR_INVALID (1) and name the fault."""
+    from cngi_prototype_gb300 import _lib
+    L = _lib.load()
+    msg = lambda: L.ngg_last_error().decode()
+    assert L.ngg_grid_ps(None, None) == 1 and 'NULL' in msg()
+    a = _lib.NggGridArgs()
+    a.n_time, a.n_baseline, a.n_chan, a.n_pol = 1, 1, 2, 1
+    assert L.ngg_grid_ps_chunk(ctypes.byref(a), 1, 2, None) == 1 and 'channel range' in msg()
+    assert L.ngg_grid_ps_chunk(ctypes.byref(a), -1, 4, None) == 1
+    assert L.ngg_predict_ps(None, None) == 1 and 'NULL' in msg()
+    assert L.ngg_degrid_ps(None, None) == 1
+    assert L.ngg_rotate_uvw(None, None, -1, 1, None, None, 1, 1, None, None, None) == 1
+    assert L.ngg_phase_rotate(None, None, 1, 1, 1, 0, None, 1, None, None) == 1 and 'dims' in msg()
+    assert L.ngg_hogbom_clean(None, None, None, 1, 8, 8, 0, 8, 0.1, 0.0, 10, 1, None, None) == 1
+    # empty work is a no-op, not an error
+    assert L.ngg_phase_rotate(None, None, 0, 5, 3, 2, None, 1, None, None) == 0
+    assert L.ngg_hogbom_clean(None, None, None, 0, 8, 8, 8, 8, 0.1, 0.0, 10, 1, None, None) == 0

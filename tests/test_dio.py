@@ -112,3 +112,22 @@ def test_codecs_that_need_numcodecs_are_refused(tmp_path):
         dio.read_xds(str(g))
     with pytest.raises(NotImplementedError, match='S3'):
         dio.read_vis('s3://bucket/obs.vis.zarr')
+
+
+@pytest.mark.gpu
+def test_make_image_from_a_store_equals_make_image_in_memory(ngg, tmp_path):
+    """A master dataset written with write_vis and read back with read_vis
+    images as the in-memory one (to the gridder's FP32 atomic order)."""
+    from conftest import load_golden
+    from cngi_prototype_gb300 import dio, xds
+    from cngi_prototype_gb300.imaging import make_image
+    d = load_golden('std_cube')
+    m = xds.mxds({'xds0': xds.vis_dataset(d['uvw'], d['vis'], d['weight'], d['freq'])})
+    dio.write_vis(m, tmp_path / 'o.vis.zarr', chunks_on_disk={'time': 8}, compressor='zlib')
+    r = dio.read_vis(tmp_path / 'o.vis.zarr')
+    gp = {'image_size': [int(x) for x in d['image_size']], 'cell_size': [float(x) for x in d['cell_arcsec']],
+          'chan_mode': 'cube', 'phase_center': [0.0, 0.0]}
+    a = make_image(m, xds.Dataset(), gp, {'xds': 'xds0'}, {})['IMAGE'].values
+    b = make_image(r, xds.Dataset(), gp, {'xds': 'xds0'}, {})['IMAGE'].values
+    assert a.shape == b.shape
+    assert np.abs(a - b).max() <= 1e-6 * np.abs(a).max()

@@ -57,6 +57,9 @@ class NggMlpScale(ctypes.Structure):
                 ('f_scale', ctypes.c_double), ('out_scale', ctypes.c_double)]
 
 
+NOALLOC_MAX_ROWS = 1048576   # include/ngg.h NGG_NOALLOC_MAX_ROWS
+NOALLOC_MAX_CHAN = 16384     # include/ngg.h NGG_NOALLOC_MAX_CHAN
+
 MLP_NPARAM = 16833
 MLP_NTRAINED = 16705
 

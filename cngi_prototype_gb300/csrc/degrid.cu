@@ -214,22 +214,61 @@ constexpr size_t kNoAllocBytes = sizeof(float4) * kNoAllocRows + sizeof(DChan) *
 static __device__ __align__(256) unsigned char g_noalloc_scratch[kNoAllocBytes];
 
 std::mutex g_noalloc_mu;
-void *g_noalloc_ptr[64] = {nullptr};
+struct NoAllocSlot {
+    unsigned long long ctx_id;   // context the address belongs to (0: none cached)
+    void *ptr;
+};
+NoAllocSlot g_noalloc_slot[64] = {};
 
-// Device address of g_noalloc_scratch on the current device (looked up once
-// per device; the host-side symbol itself is not a device address).
+// The driver's context calls, reached through the runtime so that the library
+// does not link libcuda (it must load on machines without a GPU driver).
+typedef int (*CtxGetCurrentFn)(void **ctx);
+typedef int (*CtxGetIdFn)(void *ctx, unsigned long long *id);
+
+// Unique id of the context current on this thread (0 if none, or if the
+// driver does not offer context ids: then the address is looked up per call).
+unsigned long long current_ctx_id() {
+    static CtxGetCurrentFn get_current = nullptr;
+    static CtxGetIdFn get_id = nullptr;
+    static std::once_flag once;
+    std::call_once(once, [] {
+        void *f = nullptr;
+        cudaDriverEntryPointQueryResult q;
+        if (cudaGetDriverEntryPointByVersion("cuCtxGetCurrent", &f, 12000, cudaEnableDefault, &q) == cudaSuccess &&
+            q == cudaDriverEntryPointSuccess)
+            get_current = reinterpret_cast<CtxGetCurrentFn>(f);
+        f = nullptr;
+        if (cudaGetDriverEntryPointByVersion("cuCtxGetId", &f, 12000, cudaEnableDefault, &q) == cudaSuccess &&
+            q == cudaDriverEntryPointSuccess)
+            get_id = reinterpret_cast<CtxGetIdFn>(f);
+        cudaGetLastError();
+    });
+    if (!get_current || !get_id) return 0;
+    void *ctx = nullptr;
+    unsigned long long id = 0;
+    if (get_current(&ctx) != 0 || !ctx || get_id(ctx, &id) != 0) return 0;
+    return id;
+}
+
+// Device address of g_noalloc_scratch in the current device's context. The
+// host-side symbol is not a device address; the address is looked up with
+// cudaGetSymbolAddress once per (device, context) and looked up again when
+// the context changes (after cudaDeviceReset the old address is invalid).
 int noalloc_scratch(void **out) {
     int dev = 0;
     NGG_CUDA(cudaGetDevice(&dev));
     if (dev < 0 || dev >= 64) return fail(NGG_ERR_UNSUPPORTED, "device index >= 64");
     std::lock_guard<std::mutex> lk(g_noalloc_mu);
-    if (!g_noalloc_ptr[dev]) {
+    NoAllocSlot &sl = g_noalloc_slot[dev];
+    const unsigned long long id = current_ctx_id();
+    if (id == 0 || sl.ctx_id != id || !sl.ptr) {
         void *p = nullptr;
-        cudaError_t e = cudaGetSymbolAddress(&p, g_noalloc_scratch);
+        cudaError_t e = cudaGetSymbolAddress(&p, g_noalloc_scratch);   // makes the context current if needed
         if (e != cudaSuccess) return cuda_fail(e, "cudaGetSymbolAddress(g_noalloc_scratch)");
-        g_noalloc_ptr[dev] = p;
+        sl.ptr = p;
+        sl.ctx_id = current_ctx_id();
     }
-    *out = g_noalloc_ptr[dev];
+    *out = sl.ptr;
     return NGG_OK;
 }
 }  // namespace

@@ -232,9 +232,11 @@ int ngg_predict_ps(const NggDegridArgs *args, void *stream);
  * every GPU that loads libngg.so until the process exits), so sizes are
  * limited: n_time*n_baseline <= NGG_NOALLOC_MAX_ROWS and
  * n_chan <= NGG_NOALLOC_MAX_CHAN, else NGG_ERR_INVALID. The first call on a
- * device looks up that array's device address (cudaGetSymbolAddress); make
- * that first call before any stream capture. Calls share the array: calls
- * whose GPU work overlaps (e.g. on two streams) corrupt each other. */
+ * device (and the first after its context was replaced, e.g. by
+ * cudaDeviceReset) looks up that array's device address
+ * (cudaGetSymbolAddress); make that first call before any stream capture.
+ * Calls share the array: calls whose GPU work overlaps (e.g. on two streams)
+ * corrupt each other. */
 #define NGG_NOALLOC_MAX_ROWS 1048576
 #define NGG_NOALLOC_MAX_CHAN 16384
 int ngg_degrid_ps_noalloc(const NggDegridArgs *args, void *stream);

@@ -1,9 +1,8 @@
 """Generate the golden fixtures for the standard-gridder path.
 
-Run in a container that has the reference checkout (default
-/root/reference, override with CNGI_REFERENCE_ROOT):
+Run where a checkout of the reference exists, naming its root:
 
-    python tests/golden/make_golden.py
+    CNGI_REFERENCE_ROOT=<checkout> python tests/golden/make_golden.py
 
 It runs the reference's own per-chunk functions -- _standard_grid_numpy_wrap,
 _standard_grid_psf_numpy_wrap, _standard_imaging_weight_degrid_numpy_wrap,
@@ -283,7 +282,7 @@ def clean_case():
     for name in ('ngcasa.deconvolution',):
         if name not in _sys.modules:
             m = _types.ModuleType(name)
-            m.__path__ = [os.path.join(refshim.REF, 'ngcasa/deconvolution')]
+            m.__path__ = [os.path.join(refshim._reference_root(), 'ngcasa/deconvolution')]
             _sys.modules[name] = m
     nb = _sys.modules['numba']
     nb.u4 = np.uint32

@@ -13,7 +13,14 @@ import os
 import sys
 import types
 
-REF = os.environ.get('CNGI_REFERENCE_ROOT', '/root/reference')
+def _reference_root():
+    root = os.environ.get('CNGI_REFERENCE_ROOT')
+    if not root:
+        raise RuntimeError('set CNGI_REFERENCE_ROOT to the root of a cngi_prototype checkout '
+                           '(the directory holding ngcasa/ and cngi/)')
+    if not os.path.isdir(os.path.join(root, 'ngcasa')):
+        raise RuntimeError(f'CNGI_REFERENCE_ROOT={root!r} holds no ngcasa/ package')
+    return root
 
 
 def install():
@@ -41,7 +48,7 @@ def install():
                       ('cngi', 'cngi'), ('cngi._utils', 'cngi/_utils'), ('cngi.image', 'cngi/image')]:
         if name not in sys.modules:
             m = types.ModuleType(name)
-            m.__path__ = [os.path.join(REF, rel)]
+            m.__path__ = [os.path.join(_reference_root(), rel)]
             sys.modules[name] = m
 
 

@@ -15,10 +15,10 @@ import pytest
 pytestmark = pytest.mark.gpu
 
 
-def _args(lib_mod, grid, uvw, weight, freq, cgk, dims, dl, vis):
+def _args(lib_mod, grid, uvw, weight, freq, cgk, dims, dl, vis, chan_mode=0, layout=0):
     a = lib_mod.NggDegridArgs()
-    a.chan_mode = 0
-    a.layout = 0
+    a.chan_mode = chan_mode
+    a.layout = layout
     a.support = 7
     a.oversampling = 100
     a.n_time, a.n_baseline, a.n_chan, a.n_pol = dims
@@ -33,14 +33,15 @@ def _args(lib_mod, grid, uvw, weight, freq, cgk, dims, dl, vis):
     return a
 
 
-def _case(seed, T, B, C, P, nu, nv):
+def _case(seed, T, B, C, P, nu, nv, chan_mode=0, uv_max=900.0):
     import torch
     rng = np.random.default_rng(seed)
-    grid = torch.as_tensor((rng.standard_normal((C, P, nu, nv)) + 1j * rng.standard_normal((C, P, nu, nv)))
+    CG = 1 if chan_mode == 1 else C
+    grid = torch.as_tensor((rng.standard_normal((CG, P, nu, nv)) + 1j * rng.standard_normal((CG, P, nu, nv)))
                            .astype(np.complex64), device='cuda')
-    uvw = torch.as_tensor(rng.uniform(-900, 900, (T, B, 3)), device='cuda')
+    uvw = torch.as_tensor(rng.uniform(-uv_max, uv_max, (T, B, 3)), device='cuda')
     weight = torch.as_tensor(rng.uniform(0.5, 2.0, (T, B, C, P)).astype(np.float32), device='cuda')
-    freq = torch.as_tensor(1.0e9 + 2e7 * np.arange(C), device='cuda')
+    freq = torch.as_tensor(1.0e9 + (2e7 if C < 1000 else 1e4) * np.arange(C), device='cuda')
     return grid, uvw, weight, freq
 
 
@@ -54,13 +55,21 @@ def test_noalloc_degrid_matches_allocating_entry_point():
     cgk = torch.as_tensor(_create_prolate_spheroidal_kernel_1D(100, 7), device='cuda')
     dl = [-5e-5, 5e-5]
     stream = ctypes.c_void_p(torch.cuda.current_stream().cuda_stream)
-    for seed, dims, nuv in [(1, (37, 21, 3, 2), (96, 100)), (2, (50, 10, 5, 1), (70, 64))]:
-        grid, uvw, weight, freq = _case(seed, *dims, *nuv)
+    # (seed, dims, grid size, chan_mode, layout): cube natural twice in a row
+    # with different sizes (stale scratch from the first call would show),
+    # continuum, the FFT layout, and continuum at exactly the channel limit
+    # with few rows (the channel region at the end of the array, to its last
+    # byte)
+    cases = [(1, (37, 21, 3, 2), (96, 100), 0, 0), (2, (50, 10, 5, 1), (70, 64), 0, 0),
+             (3, (23, 17, 6, 2), (80, 72), 1, 0), (4, (29, 13, 4, 2), (90, 66), 0, 1),
+             (5, (2, 3, _lib.NOALLOC_MAX_CHAN, 1), (64, 64), 1, 1)]
+    for seed, dims, nuv, cm, lay in cases:
+        grid, uvw, weight, freq = _case(seed, *dims, *nuv, chan_mode=cm, uv_max=900.0 if dims[2] < 1000 else 300.0)
         out_ref = torch.empty(dims, dtype=torch.complex64, device='cuda')
         out_new = torch.full(dims, complex(np.nan, np.nan), dtype=torch.complex64, device='cuda')
-        a = _args(_lib, grid, uvw, weight, freq, cgk, dims, dl, out_ref)
+        a = _args(_lib, grid, uvw, weight, freq, cgk, dims, dl, out_ref, cm, lay)
         assert L.ngg_degrid_ps(ctypes.byref(a), stream) == 0
-        b = _args(_lib, grid, uvw, weight, freq, cgk, dims, dl, out_new)
+        b = _args(_lib, grid, uvw, weight, freq, cgk, dims, dl, out_new, cm, lay)
         assert L.ngg_degrid_ps_noalloc(ctypes.byref(b), stream) == 0, L.ngg_last_error()
         torch.cuda.synchronize()
         r, n = out_ref.cpu().numpy(), out_new.cpu().numpy()

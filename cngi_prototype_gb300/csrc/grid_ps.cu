@@ -27,14 +27,16 @@
 //     are written as zeros; busy tiles are accumulated in shared memory and
 //     written once, coalesced. The grid is therefore written exactly once
 //     and never read back.
-//  Inside a busy tile each warp runs 8 track processors of 4 lanes. A lane
-//  owns up to two of the 7 column residue classes (Romein's work
-//  distribution) and, for each, the 7 rows of the current footprint in
-//  registers; it adds tap*tap*datum in registers while its cells stay the
-//  same and flushes a cell to shared memory (atomic add) when the track
-//  moves off it or, at the latest, every second 32-step chunk. Taps come from the oversampled table, loaded into shared
-//  memory by a TMA bulk copy. Cell and oversampling indices are certified to
-//  equal the reference's FP64 results (see cell_pair).
+//  Inside a busy tile each warp takes a contiguous range of the tile's
+//  chunks, one 32-step track chunk at a time: its lanes first turn the 32
+//  packed steps into per-step tap products (tap_u x weighted data, tap_v),
+//  then walk the steps with the 49 footprint cells owned in Romein's residue
+//  classes (a lane holds one u class and two v classes in registers),
+//  flushing a cell to shared memory (atomic add) only when the track moves
+//  off it or, at the latest, every second chunk. Taps come from the
+//  oversampled table, loaded into shared memory by a TMA bulk copy. Cell and
+//  oversampling indices are certified to equal the reference's FP64 results
+//  (see cell_pair).
 #include <cub/cub.cuh>
 
 #include <algorithm>
@@ -48,9 +50,6 @@ namespace {
 constexpr int TU = 64;      // tile rows (u)
 constexpr int TV = 64;      // tile columns (v, contiguous)
 constexpr int CH = 32;      // time steps per chunk
-constexpr int NW = 8;       // warps per CTA
-constexpr int NG = 8;       // track processors per warp (4 lanes each)
-constexpr int ROUND = 8;    // producer round length (steps)
 constexpr int SUP = 7;
 constexpr int SC = 3;
 constexpr int MAX_TAB = 4096;
@@ -76,6 +75,7 @@ struct TileArgs {
     void *grid;
     double *sum_weight;
     int *work_counter;        // [0] tile queue, [1] zero queue
+    int *err;                 // set to 1 when the table copy's bounded wait runs out
     const int *bbox;          // busy tile range (tu0, tu1, tv0, tv1) over all image channels
     const struct SubItem *subs;  // tile work items
     const int *n_subs;        // number of tile work items (device)
@@ -379,11 +379,6 @@ struct SubItem {
     int pad;
 };
 
-__device__ __forceinline__ int mod7(int x) {
-    int r = x % 7;
-    return r < 0 ? r + 7 : r;
-}
-
 __device__ __forceinline__ bool mbar_wait(unsigned addr, unsigned phase) {
     for (int it = 0; it < (1 << 22); ++it) {
         unsigned ok;
@@ -552,32 +547,56 @@ __device__ __noinline__ bool zero_next(const ZeroRows &z) {
     return true;
 }
 
-// register accumulator of one (column, row) cell
-template <bool CPLX>
-struct Cell;
-template <>
-struct Cell<true> { float2 a, b; };   // (re, im) of pol 0 and pol 1
-template <>
-struct Cell<false> { float2 a; };     // (pol 0, pol 1) of a real grid
+// ---- the tile kernel: one track per warp ------------------------------------
+//
+// A CTA owns one uv-tile (TU x TV cells, every pol of the launch) of one image
+// channel at a time, accumulated in shared memory and written to the grid
+// once. Its warps take contiguous ranges of the tile's chunk list; a warp
+// handles one 32-step chunk at a time in two phases:
+//  * producer: lane s takes step s of the chunk (its packed record, loaded
+//    from global memory one chunk ahead) and writes to the warp's shared
+//    record the 7 products tap_u(k) * weighted data (both pols), the 7 v
+//    taps of the step and the step's cell;
+//  * consumer: the 49 footprint cells are owned in Romein's residue classes:
+//    lane (kappa, g), kappa = lane % 7 the u class (u mod 7), g = lane / 7
+//    (0..3), holds the cells of u class kappa and v classes 2g and 2g+1 in
+//    registers (lanes 28-31 hold none). Every lane walks the 32 steps adding
+//    record_u[its u tap] * tap_v[its v taps] to its two cells. When the
+//    track's cell changes (a warp-uniform branch) only the cells that leave
+//    the footprint are flushed to the shared tile (atomic adds) and
+//    restarted; every second chunk all cells are flushed, so that no FP32
+//    register sum runs longer than 64 steps (long sums of like-sized terms
+//    drift). The cells are absolute grid cells, so a chunk of another track
+//    simply continues accumulating into whichever cells it shares.
+// The taps come from the oversampled table staged in shared memory by a TMA
+// bulk copy. The tile is stored as (re, im) planes per pol whose column
+// index is XOR-swizzled by the row, so the flush atomics of the 7 u classes
+// of one v cell fall into different banks.
+constexpr int NWT = 16;                  // warps per CTA
+constexpr int REC_V = 9;                 // floats per step of v taps (odd stride: conflict-free producer stores)
+constexpr int WARP_REC_BYTES = CH * SUP * 16 + CH * REC_V * 4 + CH * 4;
+
+__device__ __forceinline__ int tile_addr(int lu, int lv) { return lu * TV + (lv ^ ((lu & 7) << 2)); }
+
+__device__ __forceinline__ void red_shared(float *p, float v) {
+    asm volatile("red.shared.add.f32 [%0], %1;" ::"r"((unsigned)__cvta_generic_to_shared(p)), "f"(v) : "memory");
+}
+
+__device__ __forceinline__ int residue_cell(int lo, int cls) {   // the cell of class cls in [lo, lo + 7)
+    int r = (cls - lo) % 7;
+    if (r < 0) r += 7;
+    return lo + r;
+}
 
 template <int NP, bool CPLX, bool FFTL>
-__global__ void __launch_bounds__(NW * 32, 2) k_tiles(const TileArgs a) {
+__global__ void __launch_bounds__(NWT * 32, 1) k_tiles(const TileArgs a) {
     extern __shared__ __align__(16) unsigned char smem[];
-    // layout: acc tile | table | norm sums | records | group info | misc
-    constexpr int ACC_ELEM = CPLX ? 8 : 4;
-    constexpr int NREC = NG * ROUND;   // records per warp
+    constexpr int NPL = CPLX ? 2 * NP : NP;   // float planes of the tile
+    constexpr int NA = CPLX ? NP : 1;         // float2 accumulators per cell
     float *acc_s = reinterpret_cast<float *>(smem);
-    const size_t acc_bytes = (size_t)NP * TU * TV * ACC_ELEM;
-    float *tab = reinterpret_cast<float *>(smem + acc_bytes);
-    // per warp: the round's step records (taps, cell, info) and, double
-    // buffered, the packed steps of this round and the next (cp.async)
-    float4 *rec_tv = reinterpret_cast<float4 *>(tab + ((a.tab_bytes + 3) / 4));   // 2 per record
-    unsigned *rec_cuv = reinterpret_cast<unsigned *>(rec_tv + 2 * NW * NREC);
-    int *rec_info = reinterpret_cast<int *>(rec_cuv + NW * NREC);
-    int4 *ginfo = reinterpret_cast<int4 *>(rec_info + NW * NREC);   // (c, b, t0, valid) per group
-    float4 *raw_wv = reinterpret_cast<float4 *>(ginfo + NW * NG);    // [NW][2][NREC]
-    uint2 *raw_meta = reinterpret_cast<uint2 *>(raw_wv + NW * 2 * NREC);
-    unsigned long long *mbar = reinterpret_cast<unsigned long long *>(raw_meta + NW * 2 * NREC);
+    float *tab = acc_s + NPL * TU * TV;
+    unsigned char *recs = reinterpret_cast<unsigned char *>(tab + ((a.tab_bytes + 3) / 4));
+    unsigned long long *mbar = reinterpret_cast<unsigned long long *>(recs + (size_t)NWT * WARP_REC_BYTES);
     int *s_item = reinterpret_cast<int *>(mbar + 1);   // [kind, item]
     float4 *zbuf = reinterpret_cast<float4 *>(
         (reinterpret_cast<uintptr_t>(s_item + 2) + 15) & ~static_cast<uintptr_t>(15));
@@ -586,14 +605,14 @@ __global__ void __launch_bounds__(NW * 32, 2) k_tiles(const TileArgs a) {
     const int warp = tid >> 5, lane = tid & 31;
 
     // ---- stage the tap table with a TMA bulk copy -------------------------
-    unsigned mbar_addr = (unsigned)__cvta_generic_to_shared(mbar);
+    const unsigned mbar_addr = (unsigned)__cvta_generic_to_shared(mbar);
     if (tid == 0) {
         asm volatile("mbarrier.init.shared::cta.b64 [%0], 1;" ::"r"(mbar_addr) : "memory");
         asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
     }
     __syncthreads();
     if (tid == 0) {
-        unsigned dst = (unsigned)__cvta_generic_to_shared(tab);
+        const unsigned dst = (unsigned)__cvta_generic_to_shared(tab);
         asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;" ::"r"(mbar_addr), "r"(a.tab_bytes)
                      : "memory");
         asm volatile(
@@ -601,22 +620,28 @@ __global__ void __launch_bounds__(NW * 32, 2) k_tiles(const TileArgs a) {
             "l"(a.tab_g), "r"(a.tab_bytes), "r"(mbar_addr)
             : "memory");
     }
-    const bool tma_ok = mbar_wait(mbar_addr, 0);
-    if (!tma_ok) {  // the bounded wait ran out: fall back to plain loads
-        for (int i = tid; i < a.tab_len; i += blockDim.x) tab[i] = a.tab_g[i];
+    if (!__syncthreads_and(mbar_wait(mbar_addr, 0))) {
+        // The bounded wait ran out: report it and return once the copy has
+        // landed (or a second bounded wait has also run out).
+        if (tid == 0) {
+            atomicExch(a.err, 1);
+            mbar_wait(mbar_addr, 0);
+        }
+        __syncthreads();
+        return;
     }
-    __syncthreads();
-    for (int i = tid; i < NP * TU * TV * (CPLX ? 2 : 1); i += blockDim.x) acc_s[i] = 0.f;
+    for (int i = tid; i < NPL * TU * TV; i += blockDim.x) acc_s[i] = 0.f;
     for (int i = tid; i < ZBUF / 16; i += blockDim.x) zbuf[i] = make_float4(0.f, 0.f, 0.f, 0.f);
     asm volatile("fence.proxy.async.shared::cta;" ::: "memory");   // the bulk stores read zbuf
     __syncthreads();
     const unsigned zs = (unsigned)__cvta_generic_to_shared(zbuf);
 
+    float4 *recA = reinterpret_cast<float4 *>(recs + (size_t)warp * WARP_REC_BYTES);   // [CH][SUP]
+    float *recV = reinterpret_cast<float *>(recA + CH * SUP);                           // [CH][REC_V]
+    unsigned *recC = reinterpret_cast<unsigned *>(recV + CH * REC_V);                   // [CH]
+
     const int64_t NT = (int64_t)a.ntu * a.ntv;
     const int cu_c = (int)(a.nu / 2), cv_c = (int)(a.nv / 2);
-    const int g = lane >> 2;            // track processor in the warp
-    const int l4 = lane & 3;            // lane within the processor
-    const int ncol = (l4 < 3) ? 2 : 1;  // column classes l4 and l4+4
     const int64_t plane = a.nu * a.nv;
     const BoxMap bm = box_map(a.bbox, a.n_img, NT, a.ntv);
     const int R0 = bm.nbu ? bm.bt0 * TU : 0, R1 = bm.nbu ? min((bm.bt0 + bm.nbu) * TU, (int)a.nu) : 0;
@@ -625,13 +650,13 @@ __global__ void __launch_bounds__(NW * 32, 2) k_tiles(const TileArgs a) {
     constexpr int ZR = 8;
     const int nrb = (int)((a.nu + ZR - 1) / ZR);
     const int64_t n_zero_items = (int64_t)a.n_img * NP * nrb;
+    const int os = a.os;
 
-    int4 *my_ginfo = ginfo + warp * NG;
-    unsigned *my_cuv = rec_cuv + warp * NREC;
-    int *my_info = rec_info + warp * NREC;
-    float4 *my_tv = rec_tv + 2 * warp * NREC;
-    float4 *my_raw_wv = raw_wv + warp * 2 * NREC;
-    uint2 *my_raw_meta = raw_meta + warp * 2 * NREC;
+    // this lane's residue classes (consumer)
+    const bool act = lane < 28;
+    const int kap = lane % 7, g = lane / 7;
+    const int rho0 = 2 * g, rho1 = 2 * g + 1;
+    const bool has1 = act && g < 3;
 
     // Rows outside the busy box are zeroed by TMA bulk stores that lane 0 of
     // each warp issues, one block of rows at a time, just before the warp
@@ -639,7 +664,7 @@ __global__ void __launch_bounds__(NW * 32, 2) k_tiles(const TileArgs a) {
     // they carry overlaps the tile work instead of taking CTAs away from it.
     const ZeroRows zr{a.grid, a.nu, a.nv, a.P, a.p0, nrb, n_zero_items, R0, R1, V0, V1, cu_c, cv_c, zs,
                       &a.work_counter[1]};
-    bool zero_left = lane == 0;   // this warp's issuing lane: zero row blocks remain
+    bool zero_left = lane == 0;
     for (;;) {
         if (tid == 0) {
             const long long it = atomicAdd(&a.work_counter[0], 1);
@@ -661,239 +686,119 @@ __global__ void __launch_bounds__(NW * 32, 2) k_tiles(const TileArgs a) {
         const bool split = si.nsub > 1;
 
         if (e0 < e1) {
-            // ---------------- busy tile ----------------
+            // ---------------- busy tile: this warp's chunk range ----------------
             const int64_t n = e1 - e0;
-            const int gi = warp * NG + g;
-            const int64_t rs = e0 + (n * gi) / (NW * NG);
-            const int64_t re = e0 + (n * (gi + 1)) / (NW * NG);
-            int jmax = (int)(re - rs);
-            for (int o = 16; o > 0; o >>= 1) jmax = max(jmax, __shfl_xor_sync(0xffffffffu, jmax, o));
-            int prev_cu = -(1 << 28), prev_cv = -(1 << 28);
-            int col[2] = {-(1 << 28), -(1 << 28)};
-            bool colv[2] = {false, false};
-            Cell<CPLX> acc[2][SUP];
+            const int64_t rs = e0 + (n * warp) / NWT, re = e0 + (n * (warp + 1)) / NWT;
+            // consumer state: the lane's cells and their accumulators
+            unsigned cur = NO_CELL;
+            int ucell = -(1 << 28), vcell0 = -(1 << 28), vcell1 = -(1 << 28);
+            int lu = 0, lv0 = 0, lv1 = 0, kA = 0, kV0 = 0, kV1 = 0;
+            bool ok0 = false, ok1 = false;
+            float2 acc[2][NA];
 #pragma unroll
-            for (int j = 0; j < 2; ++j)
+            for (int r = 0; r < 2; ++r)
 #pragma unroll
-                for (int d = 0; d < SUP; ++d) {
-                    acc[j][d].a = make_float2(0.f, 0.f);
-                    if constexpr (CPLX) acc[j][d].b = make_float2(0.f, 0.f);
-                }
+                for (int q = 0; q < NA; ++q) acc[r][q] = make_float2(0.f, 0.f);
 
-            auto flush_cell = [&](int j, int d) {
-                const int row = prev_cv - SC + d;
-                if (!colv[j] || row < v0 || row >= v0 + TV || row >= a.nv) return;
-                const int lu = col[j] - u0, lv = row - v0;
-                if constexpr (CPLX) {
-                    const float2 x = acc[j][d].a;
-                    if (x.x != 0.f || x.y != 0.f) {
-                        float *q = acc_s + 2 * ((size_t)lu * TV + lv);
-                        atomicAdd(q, x.x);
-                        atomicAdd(q + 1, x.y);
+            auto flush = [&](int r) {
+                const bool ok = r ? ok1 : ok0;
+                if (!ok) return;
+                const int ad = tile_addr(lu, r ? lv1 : lv0);
+#pragma unroll
+                for (int q = 0; q < NA; ++q) {
+                    const float2 x = acc[r][q];
+                    if constexpr (CPLX) {
+                        if (x.x != 0.f) red_shared(acc_s + (2 * q) * TU * TV + ad, x.x);
+                        if (x.y != 0.f) red_shared(acc_s + (2 * q + 1) * TU * TV + ad, x.y);
+                    } else {
+                        if (x.x != 0.f) red_shared(acc_s + ad, x.x);
+                        if (NP > 1 && x.y != 0.f) red_shared(acc_s + TU * TV + ad, x.y);
                     }
-                    if (NP > 1) {
-                        const float2 y = acc[j][d].b;
-                        if (y.x != 0.f || y.y != 0.f) {
-                            float *q = acc_s + 2 * (((size_t)TU + lu) * TV + lv);
-                            atomicAdd(q, y.x);
-                            atomicAdd(q + 1, y.y);
+                }
+            };
+            auto zero = [&](int r) {
+#pragma unroll
+                for (int q = 0; q < NA; ++q) acc[r][q] = make_float2(0.f, 0.f);
+            };
+            auto change = [&](unsigned cuv) {
+                const int cu = (int)(cuv >> 16), cv = (int)(cuv & 0xffffu);
+                const int nu_ = residue_cell(cu - SC, kap);
+                const int nv0 = residue_cell(cv - SC, rho0), nv1 = residue_cell(cv - SC, rho1);
+                const bool cc = nu_ != ucell;
+                if (cc || nv0 != vcell0) { flush(0); zero(0); }
+                if (cc || nv1 != vcell1) { flush(1); zero(1); }
+                ucell = nu_; vcell0 = nv0; vcell1 = nv1;
+                lu = ucell - u0; lv0 = vcell0 - v0; lv1 = vcell1 - v0;
+                const bool in_u = act && (unsigned)lu < (unsigned)TU;
+                ok0 = in_u && (unsigned)lv0 < (unsigned)TV;
+                ok1 = in_u && has1 && (unsigned)lv1 < (unsigned)TV;
+                kA = ucell - cu + SC;
+                kV0 = vcell0 - cv + SC;
+                kV1 = vcell1 - cv + SC;
+                cur = cuv;
+            };
+
+            // the chunk j's packed step of this lane (producer), one chunk ahead
+            uint2 m_nx = make_uint2(NO_CELL, 0u);
+            float4 d_nx = make_float4(0.f, 0.f, 0.f, 0.f);
+            auto fetch = [&](int64_t j) {
+                const unsigned chu = (unsigned)(a.keys[j] & 0xffffffffull);
+                const int64_t ri = (int64_t)chu * CH + lane;
+                m_nx = __ldg(a.meta + ri);
+                d_nx = __ldg(a.wvp + ri);
+            };
+            if (rs < re) fetch(rs);
+            int jl = 0;
+            for (int64_t j = rs; j < re; ++j, ++jl) {
+                const uint2 m = m_nx;
+                const float4 d = d_nx;
+                if (j + 1 < re) fetch(j + 1);
+                // ---- producer: lane = step ----
+                {
+                    float4 *ra = recA + lane * SUP;
+                    float *rv = recV + lane * REC_V;
+                    if (m.x != NO_CELL) {
+                        const int ou = (int)(m.y & 0xffffu) - 32768, ov = (int)(m.y >> 16) - 32768;
+#pragma unroll
+                        for (int k = 0; k < SUP; ++k) {
+                            const float tu = tab[abs(os * (k - SC) + ou)];
+                            const float2 t2 = make_float2(tu, tu);
+                            const float2 lo = __fmul2_rn(t2, make_float2(d.x, d.y));
+                            const float2 hi = __fmul2_rn(t2, make_float2(d.z, d.w));
+                            ra[k] = make_float4(lo.x, lo.y, hi.x, hi.y);
+                            rv[k] = tab[abs(os * (k - SC) + ov)];
+                        }
+                    } else {
+#pragma unroll
+                        for (int k = 0; k < SUP; ++k) {
+                            ra[k] = make_float4(0.f, 0.f, 0.f, 0.f);
+                            rv[k] = 0.f;
                         }
                     }
-                } else {
-                    const float2 x = acc[j][d].a;
-                    if (x.x != 0.f) atomicAdd(acc_s + (size_t)lu * TV + lv, x.x);
-                    if (NP > 1 && x.y != 0.f) atomicAdd(acc_s + ((size_t)TU + lu) * TV + lv, x.y);
-                }
-            };
-            auto zero_cell = [&](int j, int d) {
-                acc[j][d].a = make_float2(0.f, 0.f);
-                if constexpr (CPLX) acc[j][d].b = make_float2(0.f, 0.f);
-            };
-
-            // chunk j of each group -> my_ginfo (lanes 0..NG-1)
-            auto decode = [&](int j) {
-                if (lane < NG) {
-                    const int ggi = warp * NG + lane;
-                    const int64_t grs = e0 + (n * ggi) / (NW * NG);
-                    const int64_t gre = e0 + (n * (ggi + 1)) / (NW * NG);
-                    int4 gi4 = make_int4(0, 0, 0, 0);
-                    if (grs + j < gre) {
-                        const unsigned chu = (unsigned)(a.keys[grs + j] & 0xffffffffull);
-                        const unsigned cq = chu / a.bnk;
-                        const unsigned rem = chu - cq * a.bnk;
-                        const unsigned bq = rem / (unsigned)a.nk;
-                        gi4 = make_int4((int)cq, (int)bq, (int)((rem - bq * (unsigned)a.nk) * CH), 1);
-                    }
-                    my_ginfo[lane] = gi4;
+                    recC[lane] = m.x;
                 }
                 __syncwarp();
-            };
-            // start the copies of round rnd of the current chunks into buffer buf:
-            // each lane its two packed steps (meta 8 bytes, data 16 bytes)
-            auto prefetch = [&](int rnd, int buf) {
-#pragma unroll
-                for (int k2 = 0; k2 < 2; ++k2) {
-                    // record q = s*NG + gg: the processors' records of one step are adjacent
-                    const int r = lane + 32 * k2;
-                    const int gg = r % NG, s = r / NG;
-                    const int4 gi4 = my_ginfo[gg];
-                    uint2 *dm = my_raw_meta + buf * NREC + r;
-                    if (gi4.w) {
-                        const int64_t ri = ((int64_t)gi4.x * a.B + gi4.y) * ((int64_t)a.nk * CH) + gi4.z +
-                                           rnd * ROUND + s;
-                        asm volatile("cp.async.ca.shared.global [%0], [%1], 8;" ::"r"(
-                                         (unsigned)__cvta_generic_to_shared(dm)),
-                                     "l"(a.meta + ri)
-                                     : "memory");
-                        asm volatile("cp.async.cg.shared.global [%0], [%1], 16;" ::"r"(
-                                         (unsigned)__cvta_generic_to_shared(my_raw_wv + buf * NREC + r)),
-                                     "l"(a.wvp + ri)
-                                     : "memory");
-                    } else {
-                        *dm = make_uint2(NO_CELL, 0u);
+                // ---- consumer: the chunk's 32 steps ----
+#pragma unroll 8
+                for (int s = 0; s < CH; ++s) {
+                    const unsigned cuv = recC[s];
+                    if (cuv != cur && cuv != NO_CELL) change(cuv);
+                    const float4 A = recA[s * SUP + kA];
+                    const float t0 = recV[s * REC_V + kV0], t1 = recV[s * REC_V + kV1];
+                    const float2 T0 = make_float2(t0, t0), T1 = make_float2(t1, t1);
+                    acc[0][0] = __ffma2_rn(make_float2(A.x, A.y), T0, acc[0][0]);
+                    acc[1][0] = __ffma2_rn(make_float2(A.x, A.y), T1, acc[1][0]);
+                    if constexpr (CPLX && NP > 1) {
+                        acc[0][1] = __ffma2_rn(make_float2(A.z, A.w), T0, acc[0][1]);
+                        acc[1][1] = __ffma2_rn(make_float2(A.z, A.w), T1, acc[1][1]);
                     }
                 }
-            };
-            if (jmax > 0) {
-                decode(0);
-                prefetch(0, 0);
+                // bound the register sums to two chunks (64 steps)
+                if (jl & 1) { flush(0); zero(0); flush(1); zero(1); }
+                __syncwarp();   // the producer of the next chunk overwrites the records
             }
-            asm volatile("cp.async.commit_group;" ::: "memory");
-
-            for (int j = 0; j < jmax; ++j) {
-                for (int rnd = 0; rnd < CH / ROUND; ++rnd) {
-                    const int buf = rnd & 1;   // CH / ROUND is even: round parity continues across chunks
-                    // copies of the next round overlap this one
-                    if (rnd + 1 < CH / ROUND) {
-                        prefetch(rnd + 1, buf ^ 1);
-                    } else if (j + 1 < jmax) {
-                        decode(j + 1);
-                        prefetch(0, buf ^ 1);
-                    }
-                    asm volatile("cp.async.commit_group;" ::: "memory");
-                    asm volatile("cp.async.wait_group 1;" ::: "memory");   // this round's copies are in
-                    // ---- producer: taps of this lane's two steps ----
-#pragma unroll
-                    for (int k2 = 0; k2 < 2; ++k2) {
-                        const int r = lane + 32 * k2;
-                        const uint2 m = my_raw_meta[buf * NREC + r];
-                        unsigned cuv = 0;
-                        int info = 0;
-                        float4 tva = make_float4(0.f, 0.f, 0.f, 0.f), tvb = tva;
-                        if (m.x != NO_CELL) {
-                            const int ou = (int)(m.y & 0xffffu) - 32768, ov = (int)(m.y >> 16) - 32768;
-                            cuv = m.x;
-                            info = 1 | ((ou + 1024) << 1);
-                            float tv[SUP];
-#pragma unroll
-                            for (int d = 0; d < SUP; ++d) tv[d] = tab[abs(a.os * (d - SC) + ov)];
-                            tva = make_float4(tv[0], tv[1], tv[2], tv[3]);
-                            tvb = make_float4(tv[4], tv[5], tv[6], 0.f);
-                        }
-                        my_cuv[r] = cuv;
-                        my_info[r] = info;
-                        my_tv[r] = tva;
-                        my_tv[NREC + r] = tvb;
-                    }
-                    __syncwarp();
-                    // ---- consumer: ROUND steps of this processor's chunk ----
-                    for (int s = 0; s < ROUND; ++s) {
-                        const int ri = s * NG + g;
-                        const int info = my_info[ri];
-                        if (!(info & 1)) continue;
-                        const unsigned cuv = my_cuv[ri];
-                        const int cu = (int)(cuv >> 16), cv = (int)(cuv & 0xffffu);
-                        const int ou = ((info >> 1) & 2047) - 1024;
-                        if (cu != prev_cu) {
-#pragma unroll
-                            for (int jj = 0; jj < 2; ++jj) {
-                                if (jj < ncol) {
-                                    const int nc = cu - SC + mod7(l4 + 4 * jj - (cu - SC));
-                                    if (nc != col[jj]) {
-#pragma unroll
-                                        for (int d = 0; d < SUP; ++d) { flush_cell(jj, d); zero_cell(jj, d); }
-                                        col[jj] = nc;
-                                        colv[jj] = (nc >= u0 && nc < u0 + TU && nc < a.nu);
-                                    }
-                                }
-                            }
-                            prev_cu = cu;
-                        }
-                        if (cv != prev_cv) {
-                            int delta = cv - prev_cv;
-                            if (delta >= SUP || delta <= -SUP) {
-#pragma unroll
-                                for (int jj = 0; jj < 2; ++jj)
-#pragma unroll
-                                    for (int d = 0; d < SUP; ++d) { flush_cell(jj, d); zero_cell(jj, d); }
-                                prev_cv = cv;
-                            } else {
-                                while (delta > 0) {
-#pragma unroll
-                                    for (int jj = 0; jj < 2; ++jj) {
-                                        flush_cell(jj, 0);
-#pragma unroll
-                                        for (int d = 0; d < SUP - 1; ++d) acc[jj][d] = acc[jj][d + 1];
-                                        zero_cell(jj, SUP - 1);
-                                    }
-                                    ++prev_cv;
-                                    --delta;
-                                }
-                                while (delta < 0) {
-#pragma unroll
-                                    for (int jj = 0; jj < 2; ++jj) {
-                                        flush_cell(jj, SUP - 1);
-#pragma unroll
-                                        for (int d = SUP - 1; d > 0; --d) acc[jj][d] = acc[jj][d - 1];
-                                        zero_cell(jj, 0);
-                                    }
-                                    --prev_cv;
-                                    ++delta;
-                                }
-                            }
-                        }
-                        const float4 wv = my_raw_wv[buf * NREC + ri];
-                        const float4 tva = my_tv[ri], tvb = my_tv[NREC + ri];
-                        const float tv[SUP] = {tva.x, tva.y, tva.z, tva.w, tvb.x, tvb.y, tvb.z};
-#pragma unroll
-                        for (int jj = 0; jj < 2; ++jj) {
-                            if (jj < ncol) {
-                                const float tu = tab[abs(a.os * (col[jj] - cu) + ou)];
-                                const float2 tu2 = make_float2(tu, tu);
-                                const float2 A0 = __fmul2_rn(tu2, make_float2(wv.x, wv.y));
-                                if constexpr (CPLX) {
-                                    const float2 A1 = __fmul2_rn(tu2, make_float2(wv.z, wv.w));
-#pragma unroll
-                                    for (int d = 0; d < SUP; ++d) {
-                                        const float2 t2 = make_float2(tv[d], tv[d]);
-                                        acc[jj][d].a = __ffma2_rn(A0, t2, acc[jj][d].a);
-                                        if (NP > 1) acc[jj][d].b = __ffma2_rn(A1, t2, acc[jj][d].b);
-                                    }
-                                } else {
-#pragma unroll
-                                    for (int d = 0; d < SUP; ++d)
-                                        acc[jj][d].a = __ffma2_rn(A0, make_float2(tv[d], tv[d]), acc[jj][d].a);
-                                }
-                            }
-                        }
-                    }
-                    __syncwarp();
-                }
-                // A slow track keeps adding to the same cells chunk after chunk;
-                // an FP32 running sum of hundreds of like-sized terms drifts (its
-                // rounding errors stop cancelling), so register sums are bounded
-                // to two chunks (64 steps) and the long sums run in the tile.
-                if (j & 1) {
-#pragma unroll
-                    for (int jj = 0; jj < 2; ++jj)
-#pragma unroll
-                        for (int d = 0; d < SUP; ++d) { flush_cell(jj, d); zero_cell(jj, d); }
-                }
-            }
-#pragma unroll
-            for (int jj = 0; jj < 2; ++jj)
-#pragma unroll
-                for (int d = 0; d < SUP; ++d) flush_cell(jj, d);
+            flush(0);
+            flush(1);
             if (zero_left) zero_left = zero_next<NP, (CPLX || FFTL) ? 8 : 4, FFTL>(zr);
             __syncthreads();   // every warp's cells are in the tile
         }
@@ -908,13 +813,16 @@ __global__ void __launch_bounds__(NW * 32, 2) k_tiles(const TileArgs a) {
                 const int u = u0 + r, v = v0 + cl;
                 float2 val = make_float2(0.f, 0.f);
                 if (busy) {
+                    const int ad = tile_addr(r, cl);
                     if constexpr (CPLX) {
-                        float2 *q = reinterpret_cast<float2 *>(acc_s) + e;
-                        val = *q;
-                        *q = make_float2(0.f, 0.f);
+                        float *qr = acc_s + (2 * p) * TU * TV + ad, *qi = qr + TU * TV;
+                        val = make_float2(*qr, *qi);
+                        *qr = 0.f;
+                        *qi = 0.f;
                     } else {
-                        val.x = acc_s[e];
-                        acc_s[e] = 0.f;
+                        float *q = acc_s + p * TU * TV + ad;
+                        val.x = *q;
+                        *q = 0.f;
                     }
                 }
                 if (u < a.nu && v < a.nv) {
@@ -949,24 +857,20 @@ __global__ void __launch_bounds__(NW * 32, 2) k_tiles(const TileArgs a) {
     }
 }
 
-size_t tile_smem_bytes(int np, bool cplx, int tab_bytes, int os) {
-    size_t acc = (size_t)np * TU * TV * (cplx ? 8 : 4);
-    size_t tab = (size_t)((tab_bytes + 3) / 4) * 4;
-    size_t rec = (size_t)NW * NG * ROUND * (32 + 4 + 4);       // taps, cell, info
-    size_t raw = (size_t)NW * 2 * NG * ROUND * (16 + 8);       // packed steps, two rounds
-    size_t gin = (size_t)NW * NG * 16;
-    size_t misc = 8 + 8;
-    (void)os;
-    return acc + tab + rec + gin + raw + misc + 16 + ZBUF;
+size_t tile_smem_bytes(int np, bool cplx, int tab_bytes) {
+    const size_t acc = (size_t)(cplx ? 2 * np : np) * TU * TV * 4;
+    const size_t tab = (size_t)((tab_bytes + 3) / 4) * 4;
+    const size_t rec = (size_t)NWT * WARP_REC_BYTES;
+    return acc + tab + rec + 8 + 8 + 16 + ZBUF;
 }
 
 template <int NP, bool CPLX, bool FFTL>
 int launch_tiles(const TileArgs &ta, int64_t n_bound, cudaStream_t s) {
-    size_t smem = tile_smem_bytes(NP, CPLX, ta.tab_bytes, ta.os);
+    const size_t smem = tile_smem_bytes(NP, CPLX, ta.tab_bytes);
     auto kern = k_tiles<NP, CPLX, FFTL>;
     NGG_CUDA(cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
     int per_sm = 0;
-    NGG_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, kern, NW * 32, smem));
+    NGG_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, kern, NWT * 32, smem));
     if (per_sm < 1) return fail(NGG_ERR_UNSUPPORTED, "k_tiles does not fit on an SM");
     if (n_bound > 0) {
         k_zero_split<CPLX, FFTL><<<(unsigned)n_bound, 256, 0, s>>>(ta.bin_start, ta.bbox, ta.n_img,
@@ -975,7 +879,7 @@ int launch_tiles(const TileArgs &ta, int64_t n_bound, cudaStream_t s) {
         NGG_CHECK_LAUNCH("k_zero_split");
     }
     const int grid = num_sms() * per_sm;
-    kern<<<grid, NW * 32, smem, s>>>(ta);
+    kern<<<grid, NWT * 32, smem, s>>>(ta);
     NGG_CHECK_LAUNCH("k_tiles");
     return NGG_OK;
 }
@@ -1290,6 +1194,7 @@ int grid_ps_impl(const NggGridArgs *a, int64_t c_off, int64_t c_stride, void *st
         const int np = (P - p0) >= 2 ? 2 : 1;
         ta.p0 = (int)p0;
         ta.work_counter = counter + 2 * launch;
+        ta.err = counter + 127;
         if (n_chunks > 0) {
             PackArgs pa;
             pa.vis = (const float2 *)vis_d;
@@ -1322,9 +1227,14 @@ int grid_ps_impl(const NggGridArgs *a, int64_t c_off, int64_t c_stride, void *st
         rc = np == 2 ? dispatch_tiles<2>(ta, n_bound, cplx, fftl, s) : dispatch_tiles<1>(ta, n_bound, cplx, fftl, s);
         if (rc != NGG_OK) return rc;
         p0 += np;
-        if (launch >= 63) return fail(NGG_ERR_UNSUPPORTED, "too many polarizations");
+        if (launch >= 62) return fail(NGG_ERR_UNSUPPORTED, "too many polarizations");
     }
     prof_record(2, s);
+    // the tile kernel's bounded wait for its table copy: report a time-out
+    int err = 0;
+    NGG_CUDA(cudaMemcpyAsync(&err, counter + 127, sizeof(int), cudaMemcpyDeviceToHost, s));
+    NGG_CUDA(cudaStreamSynchronize(s));
+    if (err) return fail(NGG_ERR_TIMEOUT, "k_tiles: the kernel table copy did not complete in time");
     return NGG_OK;
 }
 }  // namespace

@@ -235,7 +235,11 @@ def test_degrid_pair_at_2048_finite_differences(ngg):
     v_data = (op.degrid(x_true).to(torch.complex128) +
               torch.as_tensor(0.1 * (rng.standard_normal((T, B, C, P)) + 1j * rng.standard_normal((T, B, C, P))),
                               device='cuda')).to(torch.complex64)
-    x = torch.as_tensor(rng.uniform(0, 1e-3, (N, N, C, P)), device='cuda').requires_grad_(True)
+    # The map is linear, so its backward does not depend on x. At 2048^2 one
+    # pixel moves a visibility by ~1e-7 of the visibility of a full-image
+    # model, so a model of even 1e-3 per pixel would make the FP32 rounding of
+    # A(x +- eps delta) as large as the difference itself: x is kept at 1e-9.
+    x = torch.as_tensor(rng.uniform(0, 1e-9, (N, N, C, P)), device='cuda').requires_grad_(True)
 
     def loss(img):
         r = degrid(img, op).to(torch.complex128) - v_data.to(torch.complex128)

@@ -33,7 +33,7 @@
 //  then walk the steps with the 49 footprint cells owned in Romein's residue
 //  classes (a lane holds one u class and two v classes in registers),
 //  flushing a cell to shared memory (atomic add) only when the track moves
-//  off it or, at the latest, every second chunk. Taps come from the
+//  off it or, at the latest, at the end of the chunk. Taps come from the
 //  oversampled table, loaded into shared memory by a TMA bulk copy. Cell and
 //  oversampling indices are certified to equal the reference's FP64 results
 //  (see cell_pair).
@@ -564,8 +564,8 @@ __device__ __noinline__ bool zero_next(const ZeroRows &z) {
 //    record_u[its u tap] * tap_v[its v taps] to its two cells. When the
 //    track's cell changes (a warp-uniform branch) only the cells that leave
 //    the footprint are flushed to the shared tile (atomic adds) and
-//    restarted; every second chunk all cells are flushed, so that no FP32
-//    register sum runs longer than 64 steps (long sums of like-sized terms
+//    restarted; after every chunk all cells are flushed, so that no FP32
+//    register sum runs longer than 32 steps (long sums of like-sized terms
 //    drift). The cells are absolute grid cells, so a chunk of another track
 //    simply continues accumulating into whichever cells it shares.
 // The taps come from the oversampled table staged in shared memory by a TMA
@@ -748,8 +748,7 @@ __global__ void __launch_bounds__(NWT * 32, 1) k_tiles(const TileArgs a) {
                 d_nx = __ldg(a.wvp + ri);
             };
             if (rs < re) fetch(rs);
-            int jl = 0;
-            for (int64_t j = rs; j < re; ++j, ++jl) {
+            for (int64_t j = rs; j < re; ++j) {
                 const uint2 m = m_nx;
                 const float4 d = d_nx;
                 if (j + 1 < re) fetch(j + 1);
@@ -793,12 +792,10 @@ __global__ void __launch_bounds__(NWT * 32, 1) k_tiles(const TileArgs a) {
                         acc[1][1] = __ffma2_rn(make_float2(A.z, A.w), T1, acc[1][1]);
                     }
                 }
-                // bound the register sums to two chunks (64 steps)
-                if (jl & 1) { flush(0); zero(0); flush(1); zero(1); }
+                // bound the register sums to one chunk (32 steps)
+                flush(0); zero(0); flush(1); zero(1);
                 __syncwarp();   // the producer of the next chunk overwrites the records
             }
-            flush(0);
-            flush(1);
             if (zero_left) zero_left = zero_next<NP, (CPLX || FFTL) ? 8 : 4, FFTL>(zr);
             __syncthreads();   // every warp's cells are in the tile
         }

@@ -33,6 +33,10 @@ class NggGridArgs(ctypes.Structure):
                 ('grid', _vp), ('sum_weight', _vp)]
 
 
+class NggImagingWeights(ctypes.Structure):
+    _fields_ = [('density', _vp), ('factors', _vp), ('n_u', _i64), ('n_v', _i64), ('flag', _vp)]
+
+
 class NggDegridArgs(ctypes.Structure):
     _fields_ = [('chan_mode', ctypes.c_int), ('layout', ctypes.c_int), ('support', ctypes.c_int),
                 ('oversampling', ctypes.c_int),
@@ -68,6 +72,9 @@ SIGNATURES = {
     'ngg_version': (ctypes.c_int, []),
     'ngg_last_error': (ctypes.c_char_p, []),
     'ngg_grid_ps': (ctypes.c_int, [ctypes.POINTER(NggGridArgs), _vp]),
+    'ngg_primary_beam': (ctypes.c_int, [ctypes.c_int, _i64, _vp, _vp, _i64, _vp, _i64, _i64,
+                                        ctypes.POINTER(ctypes.c_double), _i64, _i64, ctypes.c_int, _vp, _vp]),
+    'ngg_grid_ps_weighted': (ctypes.c_int, [ctypes.POINTER(NggGridArgs), ctypes.POINTER(NggImagingWeights), _vp]),
     'ngg_grid_density': (ctypes.c_int, [ctypes.c_int, _i64, _i64, _i64, _i64, _i64, _i64,
                                         ctypes.POINTER(ctypes.c_double), _vp, _vp, _vp, _vp, _vp, _vp]),
     'ngg_briggs_factors': (ctypes.c_int, [ctypes.c_int, ctypes.c_double, ctypes.c_double, _i64, _i64, _i64,
@@ -186,7 +193,7 @@ def _pinned_or_dev(x, dtype, name):
 
 def grid_ps(vis, uvw, weight, freq, cgk_1D, n_uv, delta_lm, mode='data', chan_mode='cube',
             layout='natural', support=7, oversampling=100, grid=None, sum_weight=None, chan_offset=0,
-            chan_total=None):
+            chan_total=None, density=None, factors=None, flag=None):
     """Standard gridder on the GPU. Returns (grid, sum_weight) CUDA tensors.
 
     vis complex64 (T,B,C,P) (ignored for mode='psf'), uvw float64 (T,B,3),
@@ -195,6 +202,10 @@ def grid_ps(vis, uvw, weight, freq, cgk_1D, n_uv, delta_lm, mode='data', chan_mo
     With chan_total, vis and weight are (T,B,chan_total,P) and the call grids
     their channels [chan_offset, chan_offset + len(freq)) (ngg_grid_ps_chunk);
     they may then be pinned host tensors, read in place.
+    With density / factors (ngg_grid_density / ngg_briggs_factors outputs) the
+    weights are natural weights and the imaging weights are formed in the
+    packing pass; flag (T,B,C,P) bool leaves flagged visibilities out of DATA
+    grids (ngg_grid_ps_weighted).
     """
     torch = _torch()
     uvw_t = _dev(uvw, torch.float64, 'uvw')
@@ -234,12 +245,50 @@ def grid_ps(vis, uvw, weight, freq, cgk_1D, n_uv, delta_lm, mode='data', chan_mo
     a.cgk_1D = _ptr(k_t).value
     a.grid = _ptr(grid).value
     a.sum_weight = _ptr(sum_weight).value
-    if chan_total is None:
+    if density is not None or flag is not None:
+        if chan_total is not None:
+            raise ValueError('density/flag need the whole-cube call (no chan_total)')
+        iw = NggImagingWeights()
+        keep = []
+        if density is not None:
+            if factors is None:
+                raise ValueError('density needs factors')
+            d_t = _dev(density, torch.float32, 'density')
+            fa_t = _dev(factors, torch.float64, 'factors')
+            keep += [d_t, fa_t]
+            iw.density, iw.factors = _ptr(d_t).value, _ptr(fa_t).value
+            iw.n_u, iw.n_v = int(d_t.shape[1]), int(d_t.shape[2])
+        if flag is not None:
+            fl_t = _dev(flag, torch.uint8, 'flag')
+            if tuple(fl_t.shape) != (T, B, C, P):
+                raise ValueError('flag must have the shape of vis')
+            keep.append(fl_t)
+            iw.flag = _ptr(fl_t).value
+        _check(load().ngg_grid_ps_weighted(ctypes.byref(a), ctypes.byref(iw), _stream()), 'ngg_grid_ps_weighted')
+        del keep
+    elif chan_total is None:
         _check(load().ngg_grid_ps(ctypes.byref(a), _stream()), 'ngg_grid_ps')
     else:
         _check(load().ngg_grid_ps_chunk(ctypes.byref(a), int(chan_offset), int(chan_total), _stream()),
                'ngg_grid_ps_chunk')
     return grid, sum_weight
+
+
+def primary_beam(function, dish_diameters, blockage_diameters, freq, image_size, cell, image_center, ipower=2):
+    """Airy primary beams (n0, n1, C, n_types) float64 CUDA tensor (ngg_primary_beam)."""
+    torch = _torch()
+    if function not in ('airy', 'casa_airy'):
+        raise NggError(f"pb function must be 'airy' or 'casa_airy', got {function!r}")
+    d = _dev(np.asarray(dish_diameters, dtype=np.float64), torch.float64, 'dish')
+    b = _dev(np.asarray(blockage_diameters, dtype=np.float64), torch.float64, 'blockage')
+    f = _dev(np.asarray(freq, dtype=np.float64), torch.float64, 'freq')
+    n0, n1 = int(image_size[0]), int(image_size[1])
+    out = torch.empty((n0, n1, int(f.shape[0]), int(d.shape[0])), dtype=torch.float64, device='cuda')
+    cl = (ctypes.c_double * 2)(float(cell[0]), float(cell[1]))
+    _check(load().ngg_primary_beam(1 if function == 'casa_airy' else 0, int(d.shape[0]), _ptr(d), _ptr(b),
+                                   int(f.shape[0]), _ptr(f), n0, n1, cl, int(image_center[0]), int(image_center[1]),
+                                   int(ipower), _ptr(out), _stream()), 'ngg_primary_beam')
+    return out
 
 
 def grid_density(uvw, weight, freq, n_uv, delta_lm, chan_mode='cube'):

@@ -270,6 +270,19 @@ __global__ void k_airy(int casa, const double *dish, const double *block, int64_
     pat[id] = v;
 }
 
+// primary beam of each dish type in the image layout (l, m, freq, type):
+// the voltage pattern of k_airy raised to ipower, exactly 1 at the centre
+__global__ void k_pb_layout(const double *pat, int64_t nt, int64_t nf, int64_t n0, int64_t n1, int ipower,
+                            double *out) {
+    const int64_t id = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (id >= nt * nf * n0 * n1) return;
+    const int64_t ty = id % nt, f = (id / nt) % nf, j = (id / (nt * nf)) % n1, i = id / (nt * nf * n1);
+    const double v = pat[((ty * nf + f) * n0 + i) * n1 + j];
+    double r = v;
+    for (int k = 1; k < ipower; ++k) r *= v;
+    out[id] = r;
+}
+
 // pair product (ipower 1 or 2) into an ifftshift-ed complex buffer
 __global__ void k_pair(const double *pat, const int32_t *pairs, int64_t np, int64_t nf, int64_t n0, int64_t n1,
                        int ipower, double2 *work) {
@@ -590,6 +603,29 @@ extern "C" int ngg_grid_gcf_weight(const NggGcfArgs *a, void *stream) {
     k_wpatch<<<(unsigned)((np + 127) / 128), 128, 0, s>>>(g, a->conv_kernel, a->support, a->n_field,
                                                          ncfb, wsum, nrm_w);
     NGG_CHECK_LAUNCH("ngg_grid_gcf_weight kernels");
+    return NGG_OK;
+}
+
+extern "C" int ngg_primary_beam(int casa_model, int64_t nt, const double *dish, const double *block, int64_t nf,
+                                const double *freq, int64_t n0, int64_t n1, const double cell[2], int64_t c0,
+                                int64_t c1, int ipower, double *out, void *stream) {
+    clear_error();
+    cudaStream_t s = (cudaStream_t)stream;
+    if (nt < 1 || nf < 0 || n0 < 1 || n1 < 1 || ipower < 1 || ipower > 8 || !cell || !dish || !block || !out ||
+        (nf > 0 && !freq))
+        return fail(NGG_ERR_INVALID, "ngg_primary_beam arguments");
+    if (nf == 0) return NGG_OK;
+    ScratchList sc(s);
+    double *pat = nullptr;
+    int rc;
+    if ((rc = sc.get((void **)&pat, sizeof(double) * nt * nf * n0 * n1)) != NGG_OK) return rc;
+    const int64_t n = nt * nf * n0 * n1;
+    // out-of-grid centres leave no pixel at exactly 1 (k_airy only fixes an in-grid centre)
+    k_airy<<<(unsigned)((n + 255) / 256), 256, 0, s>>>(casa_model, dish, block, nt, freq, nf, n0, n1, cell[0], cell[1],
+                                                        c0, c1, pat);
+    NGG_CHECK_LAUNCH("k_airy");
+    k_pb_layout<<<(unsigned)((n + 255) / 256), 256, 0, s>>>(pat, nt, nf, n0, n1, ipower, out);
+    NGG_CHECK_LAUNCH("k_pb_layout");
     return NGG_OK;
 }
 

@@ -131,7 +131,53 @@ struct PackArgs {
     int64_t c_stride, c_off;  // vis/weight are (T,B,c_stride,P); this call's channels start at c_off
     int64_t nu, nv;
     int nk, p0, os;
+    // Imaging weights formed in this pass (ngg_grid_ps_weighted): the
+    // weights above are then the natural weights, divided by f0*W + f1 at
+    // the step's cell of the weight-density planes (NULL: used as given).
+    const float *density;        // (n_img, dnu, dnv)
+    const double *factors;       // (2, n_img)
+    const ChanParms *dchan;      // [C] uv scale of the density grid
+    const unsigned char *flag;   // (T,B,c_stride,P), nonzero = flagged visibility (DATA mode), or NULL
+    int64_t dnu, dnv, n_img;
+    int continuum;
 };
+
+// The reference's nearest-cell weight lookup (_standard_imaging_weight_degrid_jit,
+// _standard_grid.py:466-518), for one (time, baseline, channel): the step's
+// cell in the unpadded density grid, W there, and the imaging weight of each
+// pol from the natural weights (two pols are averaged first). false: the
+// cell lies outside the density grid (the reference gives weight 0).
+template <int NP>
+__device__ __forceinline__ bool step_imaging_weights(const PackArgs &a, float4 us, int64_t t, int64_t b, int64_t c,
+                                                     int64_t base, float (&w)[NP]) {
+    const ChanParms dp = a.dchan[c];
+    int du, dv, o;
+    if (!cell_pair(us.x, us.y, dp.suh, dp.sul, false, (int)(a.dnu / 2), 0, du, o)) {
+        long long i64, o64;
+        cell_fp64(a.uvw[(t * a.B + b) * 3 + 0], dp.su, false, (int)(a.dnu / 2), 0, i64, o64);
+        du = (int)max(min(i64, (long long)1 << 30), -((long long)1 << 30));
+    }
+    if (!cell_pair(us.z, us.w, dp.svh, dp.svl, false, (int)(a.dnv / 2), 0, dv, o)) {
+        long long i64, o64;
+        cell_fp64(a.uvw[(t * a.B + b) * 3 + 1], dp.sv, false, (int)(a.dnv / 2), 0, i64, o64);
+        dv = (int)max(min(i64, (long long)1 << 30), -((long long)1 << 30));
+    }
+    if (du < 0 || du >= a.dnu || dv < 0 || dv >= a.dnv) return false;
+    const int64_t cimg = a.continuum ? 0 : c;   // image channel of this call
+    const float W = a.density[(cimg * a.dnu + du) * a.dnv + dv];
+    const float f0 = (float)a.factors[cimg], f1 = (float)a.factors[a.n_img + cimg];
+    const bool Wok = !isnan(W) && W != 0.f;
+    const int64_t b0 = base - a.p0;   // pol 0 of this (time, baseline, channel)
+    const float avg = a.P == 2 ? (a.weight[b0] + a.weight[b0 + 1]) * 0.5f : 0.f;
+#pragma unroll
+    for (int p = 0; p < NP; ++p) {
+        const float wp = a.weight[base + p];
+        float iw = a.P == 2 ? avg : wp;
+        if (!isnan(wp) && wp != 0.f && Wok) iw = iw / (f0 * W + f1);
+        w[p] = iw;
+    }
+    return true;
+}
 
 // One pass over the visibilities (time, baseline, chan, pol): per step its
 // cell and oversampling offsets (the FP64 index chain, certified FP32 pairs),
@@ -182,13 +228,21 @@ __global__ void __launch_bounds__(256) k_pack(const PackArgs a) {
                     float w[NP];
                     bool pv[NP];
                     bool any = false;
+                    bool in_density = true;
+                    if (a.density) {
+                        in_density = step_imaging_weights<NP>(a, us, t, b, c, base, w);
+                    } else {
+#pragma unroll
+                        for (int p = 0; p < NP; ++p) w[p] = a.weight[base + p];
+                    }
 #pragma unroll
                     for (int p = 0; p < NP; ++p) {
-                        w[p] = a.weight[base + p];
+                        if (!in_density) w[p] = 0.f;
                         if constexpr (CPLX) {
                             const float2 vv = a.vis[base + p];
                             const float xr = vv.x * w[p], xi = vv.y * w[p];
                             pv[p] = !isnan(xr) && !isnan(xi) && (xr != 0.f || xi != 0.f);
+                            if (a.flag && a.flag[base + p]) pv[p] = false;   // flagged: the visibility is NaN
                             if (p == 0) { wv.x = pv[p] ? xr : 0.f; wv.y = pv[p] ? xi : 0.f; }
                             else { wv.z = pv[p] ? xr : 0.f; wv.w = pv[p] ? xi : 0.f; }
                         } else {
@@ -998,13 +1052,13 @@ int device_view(const void *p, const void **out, const char *what) {
     return NGG_OK;
 }
 
-int grid_ps_impl(const NggGridArgs *a, int64_t c_off, int64_t c_stride, void *stream);
+int grid_ps_impl(const NggGridArgs *a, int64_t c_off, int64_t c_stride, const NggImagingWeights *iw, void *stream);
 }  // namespace
 
 extern "C" int ngg_grid_ps(const NggGridArgs *a, void *stream) {
     clear_error();
     if (!a) return fail(NGG_ERR_INVALID, "args is NULL");
-    return grid_ps_impl(a, 0, a->n_chan, stream);
+    return grid_ps_impl(a, 0, a->n_chan, nullptr, stream);
 }
 
 extern "C" int ngg_grid_ps_chunk(const NggGridArgs *a, int64_t chan_offset, int64_t n_chan_total, void *stream) {
@@ -1012,11 +1066,23 @@ extern "C" int ngg_grid_ps_chunk(const NggGridArgs *a, int64_t chan_offset, int6
     if (!a) return fail(NGG_ERR_INVALID, "args is NULL");
     if (chan_offset < 0 || a->n_chan < 0 || n_chan_total < chan_offset + a->n_chan)
         return fail(NGG_ERR_INVALID, "channel range outside the input arrays");
-    return grid_ps_impl(a, chan_offset, n_chan_total, stream);
+    return grid_ps_impl(a, chan_offset, n_chan_total, nullptr, stream);
+}
+
+extern "C" int ngg_grid_ps_weighted(const NggGridArgs *a, const NggImagingWeights *iw, void *stream) {
+    clear_error();
+    if (!a || !iw) return fail(NGG_ERR_INVALID, "args is NULL");
+    if (iw->density) {
+        if (!iw->factors) return fail(NGG_ERR_INVALID, "density without Briggs factors");
+        if (iw->n_u < 1 || iw->n_v < 1 || iw->n_u > 65535 || iw->n_v > 65535)
+            return fail(NGG_ERR_INVALID, "density grid size out of [1,65535]");
+        if (a->n_pol > 2) return fail(NGG_ERR_UNSUPPORTED, "imaging weights from density: at most 2 pols");
+    }
+    return grid_ps_impl(a, 0, a->n_chan, iw, stream);
 }
 
 namespace {
-int grid_ps_impl(const NggGridArgs *a, int64_t c_off, int64_t c_stride, void *stream) {
+int grid_ps_impl(const NggGridArgs *a, int64_t c_off, int64_t c_stride, const NggImagingWeights *iw, void *stream) {
     cudaStream_t s = (cudaStream_t)stream;
     if (a->mode != NGG_MODE_DATA && a->mode != NGG_MODE_PSF) return fail(NGG_ERR_INVALID, "mode");
     if (a->chan_mode != NGG_CHAN_CUBE && a->chan_mode != NGG_CHAN_CONTINUUM) return fail(NGG_ERR_INVALID, "chan_mode");
@@ -1164,6 +1230,16 @@ int grid_ps_impl(const NggGridArgs *a, int64_t c_off, int64_t c_stride, void *st
         NGG_CHECK_LAUNCH("k_nsum");
     }
 
+    // imaging weights formed in the packing pass: per-channel scale of the density grid
+    ChanParms *dchan = nullptr;
+    const bool fused_w = iw && iw->density && n_chunks > 0;
+    if (fused_w) {
+        if ((rc = sc.get((void **)&dchan, sizeof(ChanParms) * C)) != NGG_OK) return rc;
+        k_chan<<<(int)((C + 127) / 128), 128, 0, s>>>(a->freq, (int)C, a->delta_lm[0], a->delta_lm[1], iw->n_u,
+                                                     iw->n_v, dchan);
+        NGG_CHECK_LAUNCH("k_chan (density)");
+    }
+
     TileArgs ta;
     ta.vis = (const float2 *)vis_d;
     ta.weight = (const float *)weight_d;
@@ -1207,6 +1283,14 @@ int grid_ps_impl(const NggGridArgs *a, int64_t c_off, int64_t c_stride, void *st
             pa.c_stride = c_stride; pa.c_off = c_off;
             pa.nu = nu; pa.nv = nv;
             pa.nk = nk; pa.p0 = (int)p0; pa.os = a->oversampling;
+            pa.density = fused_w ? iw->density : nullptr;
+            pa.factors = fused_w ? iw->factors : nullptr;
+            pa.dchan = dchan;
+            pa.flag = (iw && cplx) ? iw->flag : nullptr;
+            pa.dnu = fused_w ? iw->n_u : 1;
+            pa.dnv = fused_w ? iw->n_v : 1;
+            pa.n_img = n_img;
+            pa.continuum = a->chan_mode == NGG_CHAN_CONTINUUM;
             const dim3 pg((unsigned)B, (unsigned)nk, (unsigned)((C + 31) / 32)), pb(32, 8);
             if (np == 2) {
                 if (cplx) k_pack<2, true><<<pg, pb, 0, s>>>(pa); else k_pack<2, false><<<pg, pb, 0, s>>>(pa);

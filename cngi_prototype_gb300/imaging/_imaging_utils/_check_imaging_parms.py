@@ -80,6 +80,18 @@ def _check_imaging_weights_parms(p):
     return bool(ok)
 
 
+def _check_pb_parms(img_dataset, pb_parms):
+    """_check_pb_parms (_check_imaging_parms.py:148-164): function (default
+    'casa_airy'), dish and blockage diameter lists of equal length."""
+    ok = _check(pb_parms, 'function', str, default='casa_airy', acceptable=['casa_airy', 'airy'])
+    ok &= _check(pb_parms, 'list_dish_diameters', list, list_len=-1, elem_types=numbers.Number)
+    ok &= _check(pb_parms, 'list_blockage_diameters', list, list_len=-1, elem_types=numbers.Number)
+    if ok and len(pb_parms['list_dish_diameters']) != len(pb_parms['list_blockage_diameters']):
+        ok = _err('Parameter list_dish_diameters and list_blockage_diameters must be the same length.')
+    del img_dataset
+    return bool(ok)
+
+
 def _check_rotation_parms(p):
     """_check_imaging_parms.py:96-106 of the reference."""
     ok = _check(p, 'new_phase_center', None, list_len=2, elem_types=numbers.Number)

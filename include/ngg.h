@@ -103,6 +103,29 @@ int ngg_grid_ps(const NggGridArgs *args, void *stream);
  * (NGG_ERR_INVALID), as it is by ngg_grid_ps. */
 int ngg_grid_ps_chunk(const NggGridArgs *args, int64_t chan_offset, int64_t n_chan_total, void *stream);
 
+/* ngg_grid_ps_weighted: ngg_grid_ps with the imaging weights formed inside
+ * the packing pass instead of read from an IMAGING_WEIGHT array, and with
+ * flags applied to the visibilities -- the per-channel-chunk pipeline of
+ * synthesis_imaging_cube (ngcasa/imaging/synthesis_imaging_cube.py:170-308:
+ * vis[flag] = NaN, _make_imaging_weight_chunk, then the PSF and image
+ * gridding) in one pass per grid. args->weight holds the natural weights
+ * (DATA_WEIGHT). With density non-NULL each weight becomes, as in
+ * _standard_imaging_weight_degrid_jit (_standard_grid.py:466-518), the
+ * two-pol average divided by f0*W + f1 at the step's nearest cell of the
+ * unpadded density grid (0 outside it); density and factors are the outputs
+ * of ngg_grid_density and ngg_briggs_factors for the same channels. With
+ * density NULL the weights are used as given (natural weighting). flag, if
+ * non-NULL, marks visibilities left out of DATA-mode grids (the reference
+ * sets them to NaN; its PSF and weight density still use their weights).
+ * Same outputs, ownership and errors as ngg_grid_ps. */
+typedef struct NggImagingWeights {
+    const float *density;        /* float32 (Cimg, n_u, n_v) or NULL        */
+    const double *factors;       /* float64 (2, Cimg) Briggs f0, f1         */
+    int64_t n_u, n_v;            /* density grid = the unpadded image size  */
+    const uint8_t *flag;         /* uint8 (T,B,C,P), nonzero = flagged      */
+} NggImagingWeights;
+int ngg_grid_ps_weighted(const NggGridArgs *args, const NggImagingWeights *iw, void *stream);
+
 /* Cell and oversampling-offset indices as every kernel above computes them
  * (the FP32-pair evaluation with FP64 fallback): for each uvw row r and
  * channel c, idx[(r*n_chan + c)*4 + {0,1,2,3}] = (cu, cv, ou, ov), with
@@ -308,6 +331,19 @@ int ngg_gcf_kernels(int casa_model, int64_t n_types, const double *dish_diameter
                     int64_t n_freq, const double *freq, int64_t n0, int64_t n1,
                     const double cell[2], int64_t c0, int64_t c1, double *conv_kernel,
                     double *weight_conv_kernel, void *stream);
+
+/* Primary beam of each dish type on the image grid, as synthesis_imaging_cube
+ * makes it (_make_pb, synthesis_imaging_cube.py:262-277, with
+ * _airy_disk / _casa_airy_disk, _make_pb_symmetric.py:26-128): the Airy
+ * voltage pattern (CASA form for casa_model = 1, textbook obscured form for
+ * 0) of dish and blockage diameters at radius sqrt(x^2+y^2) * 2 pi f / c *
+ * dish / 2, x = (i - c0) cell[0], y = (j - c1) cell[1], raised to ipower
+ * (2: the power pattern), with the centre pixel exactly 1. dish, block:
+ * float64 (n_types) device arrays; freq float64 (n_freq). Output float64
+ * (n0, n1, n_freq, n_types). */
+int ngg_primary_beam(int casa_model, int64_t n_types, const double *dish_diameters,
+                     const double *blockage_diameters, int64_t n_freq, const double *freq, int64_t n0, int64_t n1,
+                     const double cell[2], int64_t c0, int64_t c1, int ipower, double *out, void *stream);
 
 /* Mosaic normalisation (make_image_with_gcf / make_psf_with_gcf through
  * _normalize, ngcasa/imaging/_imaging_utils/_normalize.py:14-90, forward

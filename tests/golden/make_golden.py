@@ -6,7 +6,7 @@ Run where a checkout of the reference exists, naming its root:
 
 It runs the reference's own per-chunk functions -- _standard_grid_numpy_wrap,
 _standard_grid_psf_numpy_wrap, _standard_imaging_weight_degrid_numpy_wrap,
-synthesis_imaging_cube's numpy imaging helpers, the prolate-spheroidal
+synthesis_imaging_cube's per-chunk function and numpy imaging helpers, the prolate-spheroidal
 kernel builders, the GCF helpers and direction_rotate's rotation and phasor
 functions, the Hogbom minor cycle and the PSF beam fit -- through ``refshim`` on small seeded
 synthetic inputs, and stores inputs and outputs as compressed .npz files next
@@ -322,6 +322,56 @@ def beam_case():
     np.savez_compressed(os.path.join(HERE, 'beam.npz'), psf=psf, delta=delta, ellipse_parms=parms)
 
 
+def sic_case():
+    """synthesis_imaging_cube: the reference's per-chunk function
+    (_synthesis_imaging_cube_std_chunk) on a flagged small cube with natural
+    weighting (its images, sums of weights, primary beams and PSF fit), and,
+    for Briggs 0.5, its helpers composed as the function documents it (the
+    imaging weights of _make_imaging_weight_chunk applied to the PSF and the
+    image; the reference's chunk function grids with the natural weights)."""
+    R = refshim.modules()
+    rng = np.random.default_rng(31)
+    enu = simulate.disk_layout(8, 300.0, rng)
+    uvw = simulate.earth_rotation_uvw(enu, 24, 120.0)
+    freq = 1.0e9 + np.arange(3) * 5.0e7
+    T, B = uvw.shape[:2]
+    vis = simulate.point_source_vis(uvw, freq, np.deg2rad(np.array([0.02, -0.05, 0.1])),
+                                    np.deg2rad(np.array([0.03, 0.01, -0.07])), [1.0, 0.5, 0.25], 2, 0.1,
+                                    rng).astype(np.complex64)
+    weight = rng.uniform(0.5, 2.0, (T, B, 3, 2))
+    weight[rng.random(weight.shape) < 0.02] = 0.0
+    flag = (rng.random((T, B, 3, 2)) < 0.08).astype(np.int8)
+    uvw[3, 2, :] = np.nan
+    gp = {'image_size': [64, 64], 'cell_size': [45.0, 45.0], 'chan_mode': 'cube', 'fft_padding': 1.2}
+    assert R.cp._check_grid_parms(gp)
+    pbp = {'function': 'casa_airy', 'list_dish_diameters': [12.0, 7.0], 'list_blockage_diameters': [0.75, 0.75]}
+    out = dict(vis=vis, uvw=uvw, weight=weight, flag=flag, freq=freq, image_size=np.array([64, 64]),
+               cell_arcsec=np.array([45.0, 45.0]), dish=np.array(pbp['list_dish_diameters']),
+               blockage=np.array(pbp['list_blockage_diameters']))
+    parms = {'grid_parms': copy.deepcopy(gp), 'imaging_weights_parms': {'weighting': 'natural'},
+             'pb_parms': copy.deepcopy(pbp)}
+    img, isw, psf, psw, pb, elp = R.sic._synthesis_imaging_cube_std_chunk(vis.copy(), uvw, weight, flag, freq, parms)
+    out.update(natural_image=img, natural_image_sum_weight=isw, natural_psf=psf, natural_psf_sum_weight=psw,
+               natural_pb=pb, natural_restore_parms=elp)
+    # Briggs 0.5: the helpers as documented (weights applied)
+    g = copy.deepcopy(gp)
+    g['oversampling'], g['support'] = 100, 7
+    cgk = R.gck._create_prolate_spheroidal_kernel_1D(100, 7)
+    _, corr = R.gck._create_prolate_spheroidal_kernel(100, 7, g['image_size_padded'])
+    corr = R.rp._remove_padding(corr, g['image_size'])
+    iw = R.sic._make_imaging_weight_chunk(uvw, weight, freq, copy.deepcopy(g), {'weighting': 'briggs', 'robust': 0.5})
+    vf = vis.copy()
+    vf[flag == 1] = np.nan
+    bimg, bisw = R.sic._make_image(vf, uvw, iw, freq, cgk, copy.deepcopy(g))
+    bimg = R.sic.correct_image(bimg, bisw[None, None, :, :], corr[:, :, None, None])
+    bpsf, bpsw = R.sic._make_psf(uvw, iw, freq, cgk, copy.deepcopy(g))
+    bpsf = R.sic.correct_image(bpsf, bpsw[None, None, :, :], corr[:, :, None, None])
+    out.update(briggs_imaging_weight=iw, briggs_image=bimg, briggs_image_sum_weight=bisw, briggs_psf=bpsf,
+               briggs_psf_sum_weight=bpsw)
+    np.savez_compressed(os.path.join(HERE, 'sic.npz'), **out)
+    print({k: getattr(v, 'shape', None) for k, v in out.items()})
+
+
 def time_reference(n_time=20, n_chan=4):
     """Time the reference's own _standard_grid_numpy_wrap (pure Python under
     refshim's identity numba.jit) on a subsample of the small standard cube
@@ -363,3 +413,5 @@ if __name__ == '__main__':
         clean_case()
     if len(sys.argv) == 1 or sys.argv[1] == 'beam':
         beam_case()
+    if len(sys.argv) == 1 or sys.argv[1] == 'sic':
+        sic_case()

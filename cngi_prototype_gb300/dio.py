@@ -9,9 +9,12 @@ file per chunk named by its chunk indices. A group may instead carry all of
 that metadata in one consolidated `.zmetadata` file.
 
 Supported chunk codecs: none, zlib, gzip, bz2 and lzma (the Python standard
-library's). Blosc -- the compressor the reference's writers use by default
-(write_vis.py:62, Blosc zstd) -- and array filters need numcodecs, which is
-not available here: such arrays raise NotImplementedError naming the codec.
+library's), zstd, and Blosc with its zstd, zlib or lz4 compressors and byte
+shuffle -- Blosc zstd being what the reference's writers use
+(write_vis.py:62, Blosc(cname='zstd', clevel=2, shuffle=0)). Blosc and zstd
+are decoded by this package's own readers of the published formats
+(_blosc.py, _zstd.py: RFC 8878), since numcodecs is not available here.
+Array filters are not supported (NotImplementedError naming them).
 Values are returned as stored: no CF decoding (times keep their numeric
 encoding and `units` attribute).
 """
@@ -25,6 +28,7 @@ import zlib
 
 import numpy as np
 
+from . import _blosc, _zstd
 from . import xds as _xds
 
 _DECODERS = {
@@ -32,6 +36,8 @@ _DECODERS = {
     'gzip': gzip.decompress,
     'bz2': bz2.decompress,
     'lzma': lzma.decompress,
+    'zstd': _zstd.decompress,
+    'blosc': _blosc.decompress,
 }
 
 
@@ -55,7 +61,7 @@ def _decode(raw, compressor, name):
         return raw
     cid = compressor.get('id')
     if cid not in _DECODERS:
-        raise NotImplementedError(f'{name}: chunk codec {cid!r} needs numcodecs (not available); '
+        raise NotImplementedError(f'{name}: chunk codec {cid!r} is not supported; '
                                   f'supported: none, ' + ', '.join(sorted(_DECODERS)))
     return _DECODERS[cid](raw)
 

@@ -215,11 +215,11 @@ __global__ void __launch_bounds__(128, 4) k_grid_gcf(const GArgs a) {
                 // register i takes tap row (i - m) mod S: row S - m + i of the doubled run
                 const float *q = tab + ((int64_t)oui * (a.os1 + 1) + ovi) * (2 * S) * SP + (S - m) * SP +
                                  (mycol - cu + sc);
+                const float2 w2 = make_float2(wx, wy);
 #pragma unroll
                 for (int i = 0; i < S; ++i) {
                     const float kk = __ldg(q + i * SP);
-                    acc[i].x = fmaf(kk, wx, acc[i].x);
-                    acc[i].y = fmaf(kk, wy, acc[i].y);
+                    acc[i] = __ffma2_rn(make_float2(kk, kk), w2, acc[i]);   // (re, im) in one paired FMA
                 }
             }
         }

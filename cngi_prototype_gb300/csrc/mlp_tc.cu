@@ -1,10 +1,16 @@
 // Learned-GCF network on the tcgen05 tensor cores: the four 64x64 layers of a
 // 128-sample tile run as tcgen05.mma (kind::f16, BF16 A and B from shared
 // memory, FP32 accumulator in tensor memory), issued by one thread and
-// completed through an mbarrier; the 4 warps read their 32 accumulator rows
-// back with tcgen05.ld, add the bias, apply SiLU in FP32 and write the next
-// layer's operand. Fourier features and the output layer are FP32 on the
-// CUDA cores.
+// completed through an mbarrier; the tile's 4 warps read their 32
+// accumulator rows back with tcgen05.ld, add the bias, apply SiLU in FP32 and
+// write the next layer's operand. Fourier features and the output layer are
+// FP32 on the CUDA cores.
+//
+// A CTA holds one copy of the weights and NG = 4 tile groups of 4 warps, each
+// with its own activation buffer, 64 TMEM columns, mbarrier and named
+// barrier: while one group's MMAs run on the tensor pipe the other groups do
+// their SiLU / feature work, so the tensor pipe and the CUDA cores overlap
+// (the CUDA-core work per tile is far larger than the MMAs').
 //
 // Split BF16: every operand is stored as hi = bf16(v) and lo = bf16(v - hi),
 // and each K-step issues hi*hi + lo*hi + hi*lo into the FP32 accumulator
@@ -26,12 +32,14 @@
 namespace ngg {
 namespace {
 
-constexpr int TC_THREADS = 128;
-constexpr int SMEM_A = 2 * 128 * 64 * 2;    // hi, lo: 32 KB
-constexpr int SMEM_B = 2 * 4 * 64 * 64 * 2; // hi, lo of W1..W4: 64 KB
+constexpr int NGRP = 4;                      // tile groups per CTA
+constexpr int TC_THREADS = 128 * NGRP;
+constexpr int SMEM_A1 = 2 * 128 * 64 * 2;    // one group's activations, hi and lo: 32 KB
+constexpr int SMEM_A = NGRP * SMEM_A1;
+constexpr int SMEM_B = 2 * 4 * 64 * 64 * 2;  // hi, lo of W1..W4: 64 KB
 constexpr int SMEM_F = (4 * 64 + 64 + 8) * 4;
-constexpr int SMEM_TOTAL = SMEM_A + SMEM_B + SMEM_F + 64;
-constexpr uint32_t TMEM_COLS = 64;
+constexpr int SMEM_TOTAL = SMEM_A + SMEM_B + SMEM_F + 128;
+constexpr uint32_t TMEM_COLS = 64 * NGRP;
 // instruction descriptor, kind::f16: D F32 (bit 4), A BF16 (bits 7-9), B BF16
 // (bits 10-12), both K-major, N >> 3 at bits 17-22, M >> 4 at bits 24-28
 constexpr uint32_t IDESC = (1u << 4) | (1u << 7) | (1u << 10) | ((64u >> 3) << 17) | ((128u >> 4) << 24);
@@ -116,7 +124,18 @@ __device__ __forceinline__ void store_row(uint8_t *hi, uint8_t *lo, int row, con
     for (int j = 0; j < 8; ++j) store8(hi, lo, (row >> 3) * 1024 + j * 128 + (row & 7) * 16, v + 8 * j);
 }
 
-__device__ __forceinline__ float silu_f(float a) { return a / (1.0f + __expf(-a)); }
+// SiLU with the fast exponential and division (each within a few ulps; the
+// split-BF16 operands carry ~2^-16 relative error): the argument of the
+// exponential is capped so 1 + e stays below 2^126, where __fdividef is exact
+__device__ __forceinline__ float silu_f(float a) { return __fdividef(a, 1.0f + __expf(fminf(-a, 80.0f))); }
+
+// (sin, cos)(2 pi d): reduced to t = d - rint(d) in [-1/2, 1/2] first (exact),
+// so the hardware sine and cosine see arguments in [-pi, pi], where their
+// absolute error is ~2^-21
+__device__ __forceinline__ void sincos_turns(float d, float *sv, float *cv) {
+    const float t = d - rintf(d);
+    __sincosf(6.283185307179586f * t, sv, cv);
+}
 
 // samples from an array: z[s] -> y[s]
 struct GenArray {
@@ -176,16 +195,22 @@ struct GenTable {
     }
 };
 
+__device__ __forceinline__ void group_sync(int grp) {
+    asm volatile("bar.sync %0, 128;" ::"r"(grp + 1) : "memory");
+}
+
 template <class Gen>
-__global__ void __launch_bounds__(TC_THREADS) k_mlp_tc(const float *params, Gen gen, int64_t n, int *err) {
+__global__ void __launch_bounds__(TC_THREADS, 1) k_mlp_tc(const float *params, Gen gen, int64_t n, int *err) {
     extern __shared__ __align__(1024) uint8_t smem[];
-    uint8_t *sA = smem, *sAl = smem + SMEM_A / 2;             // activations hi / lo
-    uint8_t *sB = smem + SMEM_A, *sBl = smem + SMEM_A + SMEM_B / 2;   // weights hi / lo
-    float *sb = reinterpret_cast<float *>(smem + SMEM_A + SMEM_B);   // b1..b4 [4][64], Wo [64], bo
-    uint64_t *bar = reinterpret_cast<uint64_t *>(smem + SMEM_A + SMEM_B + SMEM_F);
-    uint32_t *s_tmem = reinterpret_cast<uint32_t *>(bar + 1);
-    int *s_fail = reinterpret_cast<int *>(bar + 2);
     const int tid = threadIdx.x, warp = tid >> 5;
+    const int grp = tid >> 7, gt = tid & 127;       // tile group, thread within the group
+    uint8_t *sA = smem + grp * SMEM_A1, *sAl = sA + SMEM_A1 / 2;   // this group's activations hi / lo
+    uint8_t *sB = smem + SMEM_A, *sBl = smem + SMEM_A + SMEM_B / 2;  // weights hi / lo
+    float *sb = reinterpret_cast<float *>(smem + SMEM_A + SMEM_B);  // b1..b4 [4][64], Wo [64], bo
+    uint64_t *bars = reinterpret_cast<uint64_t *>(smem + SMEM_A + SMEM_B + SMEM_F);   // [NGRP]
+    uint32_t *s_tmem = reinterpret_cast<uint32_t *>(bars + NGRP);
+    int *s_fail = reinterpret_cast<int *>(bars + NGRP + 1);                             // [NGRP]
+    uint64_t *bar = bars + grp;
 
     // weights as B operands (N = output, K = input), biases, output layer
     for (int e = tid; e < 4 * 64 * 8; e += TC_THREADS) {
@@ -197,11 +222,11 @@ __global__ void __launch_bounds__(TC_THREADS) k_mlp_tc(const float *params, Gen 
     }
     for (int e = tid; e < 4 * 64; e += TC_THREADS) sb[e] = params[(e / 64) * MLP_LAYER + 4096 + e % 64];
     for (int e = tid; e < 65; e += TC_THREADS) sb[256 + e] = params[MLP_OFF_WO + e];
-    if (tid == 0) {
-        asm volatile("mbarrier.init.shared::cta.b64 [%0], 1;" ::"r"(smem_u32(bar)) : "memory");
-        asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
-        *s_fail = 0;
+    if (tid < NGRP) {
+        asm volatile("mbarrier.init.shared::cta.b64 [%0], 1;" ::"r"(smem_u32(bars + tid)) : "memory");
+        s_fail[tid] = 0;
     }
+    if (tid == 0) asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
     if (warp == 0) {
         asm volatile("tcgen05.alloc.cta_group::1.sync.aligned.shared::cta.b32 [%0], %1;" ::"r"(smem_u32(s_tmem)),
                      "r"(TMEM_COLS)
@@ -213,12 +238,15 @@ __global__ void __launch_bounds__(TC_THREADS) k_mlp_tc(const float *params, Gen 
     __syncthreads();
     fence_after();
     const uint32_t tbase = *s_tmem;
-    const uint32_t trow = tbase + ((uint32_t)(warp * 32) << 16);
+    const uint32_t tcol = tbase + (uint32_t)(64 * grp);                 // this group's accumulator
+    const uint32_t trow = tcol + ((uint32_t)((warp & 3) * 32) << 16);   // this warp's 32 lanes
     const float *Bf = params + MLP_OFF_B;
     uint32_t parity = 0;
+    bool failed = false;
 
-    for (int64_t tile = blockIdx.x; tile * 128 < n; tile += gridDim.x) {
-        const int64_t s = tile * 128 + tid;
+    for (int64_t tile = (int64_t)blockIdx.x * NGRP + grp; tile * 128 < n && !failed;
+         tile += (int64_t)gridDim.x * NGRP) {
+        const int64_t s = tile * 128 + gt;
         float h[64];
         {
             float x = 0.f, y = 0.f, f = 0.f;
@@ -227,31 +255,30 @@ __global__ void __launch_bounds__(TC_THREADS) k_mlp_tc(const float *params, Gen 
 #pragma unroll
             for (int j = 0; j < 32; ++j) {
                 const float d = Bf[j * 4] * x + Bf[j * 4 + 1] * y + Bf[j * 4 + 2] * r + Bf[j * 4 + 3] * f;
-                sincospif(2.0f * d, &h[j], &h[32 + j]);
+                sincos_turns(d, &h[j], &h[32 + j]);
             }
-            store_row(sA, sAl, tid, h);
+            store_row(sA, sAl, gt, h);
         }
         fence_async_smem();
         fence_before();
-        __syncthreads();
+        group_sync(grp);
         fence_after();
-        bool failed = false;
         for (int layer = 0; layer < 4; ++layer) {
-            if (tid == 0) {
+            if (gt == 0) {
                 const uint32_t a0 = smem_u32(sA), a1 = smem_u32(sAl);
                 const uint32_t b0 = smem_u32(sB + layer * 8192), b1 = smem_u32(sBl + layer * 8192);
 #pragma unroll
                 for (int kk = 0; kk < 4; ++kk) {
                     const uint64_t ah = sdesc(a0 + kk * 256, 128, 1024), al = sdesc(a1 + kk * 256, 128, 1024);
                     const uint64_t bh = sdesc(b0 + kk * 256, 128, 1024), bl = sdesc(b1 + kk * 256, 128, 1024);
-                    mma_bf16(tbase, ah, bh, kk > 0 ? 1u : 0u);
-                    mma_bf16(tbase, al, bh, 1u);
-                    mma_bf16(tbase, ah, bl, 1u);
+                    mma_bf16(tcol, ah, bh, kk > 0 ? 1u : 0u);
+                    mma_bf16(tcol, al, bh, 1u);
+                    mma_bf16(tcol, ah, bl, 1u);
                 }
                 commit(bar);
             }
             if (!bar_wait(bar, parity)) {
-                *s_fail = 1;
+                s_fail[grp] = 1;
                 atomicExch(err, 1);
             }
             parity ^= 1u;
@@ -265,13 +292,13 @@ __global__ void __launch_bounds__(TC_THREADS) k_mlp_tc(const float *params, Gen 
 #pragma unroll
             for (int j = 0; j < 64; ++j) h[j] = silu_f(__uint_as_float(acc[j]) + sb[layer * 64 + j]);
             if (layer < 3) {
-                store_row(sA, sAl, tid, h);
+                store_row(sA, sAl, gt, h);
                 fence_async_smem();
             }
             fence_before();
-            __syncthreads();
+            group_sync(grp);
             fence_after();
-            if (*s_fail) {
+            if (s_fail[grp]) {
                 failed = true;
                 break;
             }
@@ -282,6 +309,7 @@ __global__ void __launch_bounds__(TC_THREADS) k_mlp_tc(const float *params, Gen 
         for (int j = 0; j < 64; ++j) out = fmaf(sb[256 + j], h[j], out);
         if (s < n) gen.store(s, out);
     }
+    if (failed && gt == 0) bar_wait(bar, parity ^ 1u);   // the timed-out MMAs' phase, another bounded wait
     fence_before();
     __syncthreads();
     fence_after();
@@ -304,7 +332,8 @@ int launch_tc(const float *params, const Gen &gen, int64_t n, cudaStream_t s) {
     if ((rc = sc.get((void **)&err, sizeof(int))) != NGG_OK) return rc;
     NGG_CUDA(cudaMemsetAsync(err, 0, sizeof(int), s));
     const int64_t tiles = (n + 127) / 128;
-    const int64_t grid = tiles < (int64_t)num_sms() * 2 ? tiles : (int64_t)num_sms() * 2;
+    const int64_t groups = (tiles + NGRP - 1) / NGRP;   // one CTA (NGRP tile groups) per SM
+    const int64_t grid = groups < (int64_t)num_sms() ? groups : (int64_t)num_sms();
     k_mlp_tc<Gen><<<(unsigned)grid, TC_THREADS, SMEM_TOTAL, s>>>(params, gen, n, err);
     NGG_CHECK_LAUNCH("k_mlp_tc");
     int herr = 0;

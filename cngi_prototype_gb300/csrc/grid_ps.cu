@@ -502,18 +502,18 @@ __global__ void k_fill_subs(const int *nsub, const int *off, int64_t n_bound, Su
 }
 
 // zero the destination of bins split over several work items (they add
-// their partial tiles with atomics)
+// their partial tiles with atomics); grid-stride over the busy box's items
+// (a few of the ~10^6 bins are split: one block per bin was all launch cost)
 template <bool CPLX, bool FFTL>
 __global__ void k_zero_split(const int64_t *bin_start, const int *bbox, int n_img, int64_t NT, int ntv,
                              int64_t n_bound, void *grid, int64_t P, int p0, int np, int64_t nu, int64_t nv) {
-    const int64_t i = blockIdx.x;
-    if (i >= n_bound) return;
     const BoxMap m = box_map(bbox, n_img, NT, ntv);
-    if (i >= (int64_t)m.nbu * m.nbv * n_img) return;
+    const int64_t n_box = (int64_t)m.nbu * m.nbv * n_img;
+    for (int64_t i = blockIdx.x; i < n_bound && i < n_box; i += gridDim.x) {
     int tiu, tiv, cimg;
     int64_t bin;
     m.map(i, tiu, tiv, cimg, bin);
-    if (bin_start[bin + 1] - bin_start[bin] <= MAXE) return;
+    if (bin_start[bin + 1] - bin_start[bin] <= MAXE) continue;
     const int u0 = tiu * TU, v0 = tiv * TV;
     const int cu_c = (int)(nu / 2), cv_c = (int)(nv / 2);
     for (int e = threadIdx.x; e < np * TU * TV; e += blockDim.x) {
@@ -527,6 +527,7 @@ __global__ void k_zero_split(const int64_t *bin_start, const int *bbox, int n_im
         const int64_t off = (((int64_t)cimg * P + p0 + p) * nu + u) * nv + v;
         if (CPLX || FFTL) reinterpret_cast<float2 *>(grid)[off] = make_float2(0.f, 0.f);
         else reinterpret_cast<float *>(grid)[off] = 0.f;
+    }
     }
 }
 
@@ -792,20 +793,26 @@ __global__ void __launch_bounds__(NWT * 32, 1) k_tiles(const TileArgs a) {
                 cur = cuv;
             };
 
-            // the chunk j's packed step of this lane (producer), one chunk ahead
+            // the chunk j's packed step of this lane (producer), loaded one
+            // chunk ahead; the chunk keys two chunks ahead, so that a data
+            // load never waits for the key load it depends on
             uint2 m_nx = make_uint2(NO_CELL, 0u);
             float4 d_nx = make_float4(0.f, 0.f, 0.f, 0.f);
-            auto fetch = [&](int64_t j) {
-                const unsigned chu = (unsigned)(a.keys[j] & 0xffffffffull);
+            unsigned key_nx = 0;
+            auto fetch = [&](unsigned chu) {
                 const int64_t ri = (int64_t)chu * CH + lane;
                 m_nx = __ldg(a.meta + ri);
                 d_nx = __ldg(a.wvp + ri);
             };
-            if (rs < re) fetch(rs);
+            if (rs < re) fetch((unsigned)(__ldg(a.keys + rs) & 0xffffffffull));
+            if (rs + 1 < re) key_nx = (unsigned)(__ldg(a.keys + rs + 1) & 0xffffffffull);
             for (int64_t j = rs; j < re; ++j) {
                 const uint2 m = m_nx;
                 const float4 d = d_nx;
-                if (j + 1 < re) fetch(j + 1);
+                if (j + 1 < re) {
+                    fetch(key_nx);
+                    if (j + 2 < re) key_nx = (unsigned)(__ldg(a.keys + j + 2) & 0xffffffffull);
+                }
                 // ---- producer: lane = step ----
                 {
                     float4 *ra = recA + lane * SUP;
@@ -924,7 +931,8 @@ int launch_tiles(const TileArgs &ta, int64_t n_bound, cudaStream_t s) {
     NGG_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, kern, NWT * 32, smem));
     if (per_sm < 1) return fail(NGG_ERR_UNSUPPORTED, "k_tiles does not fit on an SM");
     if (n_bound > 0) {
-        k_zero_split<CPLX, FFTL><<<(unsigned)n_bound, 256, 0, s>>>(ta.bin_start, ta.bbox, ta.n_img,
+        const int64_t zb = n_bound < (int64_t)num_sms() * 16 ? n_bound : (int64_t)num_sms() * 16;
+        k_zero_split<CPLX, FFTL><<<(unsigned)zb, 256, 0, s>>>(ta.bin_start, ta.bbox, ta.n_img,
                                                                     (int64_t)ta.ntu * ta.ntv, ta.ntv, n_bound,
                                                                     ta.grid, ta.P, ta.p0, NP, ta.nu, ta.nv);
         NGG_CHECK_LAUNCH("k_zero_split");
@@ -1171,13 +1179,16 @@ int grid_ps_impl(const NggGridArgs *a, int64_t c_off, int64_t c_stride, const Ng
             k_emit<<<nb, 256, 0, s>>>(bbox, chan, C, B, nk, nu, nv, ntu, ntv,
                                        a->chan_mode == NGG_CHAN_CONTINUUM, offsets, keys);
             NGG_CHECK_LAUNCH("k_emit");
+            // k_emit writes each chunk's keys in chunk order, so a stable
+            // sort on the bin bits alone (LSD radix sort is stable) leaves
+            // every bin's chunks in (chan, baseline, time) order
             int end_bit = 32;
             while (end_bit < 64 && ((unsigned long long)n_bins >> (end_bit - 32)) > 0) ++end_bit;
             size_t sort_bytes = 0;
-            NGG_CUDA(cub::DeviceRadixSort::SortKeys(nullptr, sort_bytes, keys, keys_sorted, n_keys, 0, end_bit, s));
+            NGG_CUDA(cub::DeviceRadixSort::SortKeys(nullptr, sort_bytes, keys, keys_sorted, n_keys, 32, end_bit, s));
             void *stmp = nullptr;
             if ((rc = sc.get(&stmp, sort_bytes)) != NGG_OK) return rc;
-            NGG_CUDA(cub::DeviceRadixSort::SortKeys(stmp, sort_bytes, keys, keys_sorted, n_keys, 0, end_bit, s));
+            NGG_CUDA(cub::DeviceRadixSort::SortKeys(stmp, sort_bytes, keys, keys_sorted, n_keys, 32, end_bit, s));
         }
     }
     k_bounds<<<(unsigned)((n_bins + 1 + 255) / 256), 256, 0, s>>>(keys_sorted, n_keys, n_bins, bin_start);

@@ -186,7 +186,7 @@ __device__ __forceinline__ bool step_imaging_weights(const PackArgs &a, float4 u
 // as one contiguous run however many tiles the chunk touches. A block is 32
 // channels x 32 steps of one (baseline, chunk): the reads are contiguous over
 // channels, a shared-memory transpose makes the writes contiguous over time.
-template <int NP, bool CPLX>
+template <int NP, bool CPLX, bool FUSED>
 __global__ void __launch_bounds__(256) k_pack(const PackArgs a) {
     __shared__ uint2 s_meta[32][33];
     __shared__ float4 s_wv[32][33];
@@ -229,8 +229,12 @@ __global__ void __launch_bounds__(256) k_pack(const PackArgs a) {
                     bool pv[NP];
                     bool any = false;
                     bool in_density = true;
-                    if (a.density) {
-                        in_density = step_imaging_weights<NP>(a, us, t, b, c, base, w);
+                    if constexpr (FUSED) {
+                        if (a.density) in_density = step_imaging_weights<NP>(a, us, t, b, c, base, w);
+                        else {
+#pragma unroll
+                            for (int p = 0; p < NP; ++p) w[p] = a.weight[base + p];
+                        }
                     } else {
 #pragma unroll
                         for (int p = 0; p < NP; ++p) w[p] = a.weight[base + p];
@@ -242,7 +246,7 @@ __global__ void __launch_bounds__(256) k_pack(const PackArgs a) {
                             const float2 vv = a.vis[base + p];
                             const float xr = vv.x * w[p], xi = vv.y * w[p];
                             pv[p] = !isnan(xr) && !isnan(xi) && (xr != 0.f || xi != 0.f);
-                            if (a.flag && a.flag[base + p]) pv[p] = false;   // flagged: the visibility is NaN
+                            if (FUSED && a.flag && a.flag[base + p]) pv[p] = false;   // flagged: the visibility is NaN
                             if (p == 0) { wv.x = pv[p] ? xr : 0.f; wv.y = pv[p] ? xi : 0.f; }
                             else { wv.z = pv[p] ? xr : 0.f; wv.w = pv[p] ? xi : 0.f; }
                         } else {
@@ -610,16 +614,19 @@ __device__ __noinline__ bool zero_next(const ZeroRows &z) {
 // handles one 32-step chunk at a time in two phases:
 //  * producer: lane s takes step s of the chunk (its packed record, loaded
 //    from global memory one chunk ahead) and writes to the warp's shared
-//    record the 7 products tap_u(k) * weighted data (both pols), the 7 v
-//    taps of the step and the step's cell;
+//    record, in residue-class order, the 7 products tap_u(k) * weighted data
+//    (both pols) and the 7 v taps (each duplicated into a pair), plus the
+//    step's cell: the product for u tap k goes to class (cu - 3 + k) mod 7,
+//    the class whose cell that tap reaches;
 //  * consumer: the 49 footprint cells are owned in Romein's residue classes:
 //    lane (kappa, g), kappa = lane % 7 the u class (u mod 7), g = lane / 7
 //    (0..3), holds the cells of u class kappa and v classes 2g and 2g+1 in
-//    registers (lanes 28-31 hold none). Every lane walks the 32 steps adding
-//    record_u[its u tap] * tap_v[its v taps] to its two cells. When the
-//    track's cell changes (a warp-uniform branch) only the cells that leave
-//    the footprint are flushed to the shared tile (atomic adds) and
-//    restarted; after every chunk all cells are flushed, so that no FP32
+//    registers (lanes 28-31 hold none). Thanks to the class order a lane
+//    reads the same record slots at every step -- one 16-byte load of its u
+//    product, one of its two v taps -- and adds them with four paired FMAs.
+//    When the track's cell changes (a warp-uniform branch) only the cells
+//    that leave the footprint are flushed to the shared tile (atomic adds)
+//    and restarted; after every chunk all cells are flushed, so that no FP32
 //    register sum runs longer than 32 steps (long sums of like-sized terms
 //    drift). The cells are absolute grid cells, so a chunk of another track
 //    simply continues accumulating into whichever cells it shares.
@@ -627,9 +634,9 @@ __device__ __noinline__ bool zero_next(const ZeroRows &z) {
 // bulk copy. The tile is stored as (re, im) planes per pol whose column
 // index is XOR-swizzled by the row, so the flush atomics of the 7 u classes
 // of one v cell fall into different banks.
-constexpr int NWT = 16;                  // warps per CTA
-constexpr int REC_V = 9;                 // floats per step of v taps (odd stride: conflict-free producer stores)
-constexpr int WARP_REC_BYTES = CH * SUP * 16 + CH * REC_V * 4 + CH * 4;
+constexpr int NWT = 24;                  // warps per CTA (one CTA per SM)
+constexpr int RT = 10;                   // float2 per step of v-tap pairs (16-byte rows; 8 used)
+constexpr int WARP_REC_BYTES = CH * SUP * 16 + CH * RT * 8 + CH * 4;
 
 __device__ __forceinline__ int tile_addr(int lu, int lv) { return lu * TV + (lv ^ ((lu & 7) << 2)); }
 
@@ -637,10 +644,9 @@ __device__ __forceinline__ void red_shared(float *p, float v) {
     asm volatile("red.shared.add.f32 [%0], %1;" ::"r"((unsigned)__cvta_generic_to_shared(p)), "f"(v) : "memory");
 }
 
-__device__ __forceinline__ int residue_cell(int lo, int cls) {   // the cell of class cls in [lo, lo + 7)
-    int r = (cls - lo) % 7;
-    if (r < 0) r += 7;
-    return lo + r;
+// the cell of class cls (0..7) in [lo, lo + 7), lo in [0, 65535]
+__device__ __forceinline__ int residue_cell(int lo, int cls) {
+    return lo + (int)((unsigned)(cls - lo + 7 * 9363) % 7u);
 }
 
 template <int NP, bool CPLX, bool FFTL>
@@ -691,9 +697,9 @@ __global__ void __launch_bounds__(NWT * 32, 1) k_tiles(const TileArgs a) {
     __syncthreads();
     const unsigned zs = (unsigned)__cvta_generic_to_shared(zbuf);
 
-    float4 *recA = reinterpret_cast<float4 *>(recs + (size_t)warp * WARP_REC_BYTES);   // [CH][SUP]
-    float *recV = reinterpret_cast<float *>(recA + CH * SUP);                           // [CH][REC_V]
-    unsigned *recC = reinterpret_cast<unsigned *>(recV + CH * REC_V);                   // [CH]
+    float4 *recA = reinterpret_cast<float4 *>(recs + (size_t)warp * WARP_REC_BYTES);   // [CH][SUP] by u class
+    float2 *recT = reinterpret_cast<float2 *>(recA + CH * SUP);                         // [CH][RT] by v class
+    unsigned *recC = reinterpret_cast<unsigned *>(recT + CH * RT);                      // [CH]
 
     const int64_t NT = (int64_t)a.ntu * a.ntv;
     const int cu_c = (int)(a.nu / 2), cv_c = (int)(a.nv / 2);
@@ -712,6 +718,7 @@ __global__ void __launch_bounds__(NWT * 32, 1) k_tiles(const TileArgs a) {
     const int kap = lane % 7, g = lane / 7;
     const int rho0 = 2 * g, rho1 = 2 * g + 1;
     const bool has1 = act && g < 3;
+    const int gr = g < 3 ? g : 3;   // lanes 28-31 read a valid slot (and never flush)
 
     // Rows outside the busy box are zeroed by TMA bulk stores that lane 0 of
     // each warp issues, one block of rows at a time, just before the warp
@@ -747,7 +754,7 @@ __global__ void __launch_bounds__(NWT * 32, 1) k_tiles(const TileArgs a) {
             // consumer state: the lane's cells and their accumulators
             unsigned cur = NO_CELL;
             int ucell = -(1 << 28), vcell0 = -(1 << 28), vcell1 = -(1 << 28);
-            int lu = 0, lv0 = 0, lv1 = 0, kA = 0, kV0 = 0, kV1 = 0;
+            int lu = 0, lv0 = 0, lv1 = 0;
             bool ok0 = false, ok1 = false;
             float2 acc[2][NA];
 #pragma unroll
@@ -776,9 +783,9 @@ __global__ void __launch_bounds__(NWT * 32, 1) k_tiles(const TileArgs a) {
                 for (int q = 0; q < NA; ++q) acc[r][q] = make_float2(0.f, 0.f);
             };
             auto change = [&](unsigned cuv) {
-                const int cu = (int)(cuv >> 16), cv = (int)(cuv & 0xffffu);
-                const int nu_ = residue_cell(cu - SC, kap);
-                const int nv0 = residue_cell(cv - SC, rho0), nv1 = residue_cell(cv - SC, rho1);
+                const int lo_u = (int)(cuv >> 16) - SC, lo_v = (int)(cuv & 0xffffu) - SC;
+                const int nu_ = residue_cell(lo_u, kap);
+                const int nv0 = residue_cell(lo_v, rho0), nv1 = residue_cell(lo_v, rho1);
                 const bool cc = nu_ != ucell;
                 if (cc || nv0 != vcell0) { flush(0); zero(0); }
                 if (cc || nv1 != vcell1) { flush(1); zero(1); }
@@ -787,9 +794,6 @@ __global__ void __launch_bounds__(NWT * 32, 1) k_tiles(const TileArgs a) {
                 const bool in_u = act && (unsigned)lu < (unsigned)TU;
                 ok0 = in_u && (unsigned)lv0 < (unsigned)TV;
                 ok1 = in_u && has1 && (unsigned)lv1 < (unsigned)TV;
-                kA = ucell - cu + SC;
-                kV0 = vcell0 - cv + SC;
-                kV1 = vcell1 - cv + SC;
                 cur = cuv;
             };
 
@@ -806,6 +810,8 @@ __global__ void __launch_bounds__(NWT * 32, 1) k_tiles(const TileArgs a) {
             };
             if (rs < re) fetch((unsigned)(__ldg(a.keys + rs) & 0xffffffffull));
             if (rs + 1 < re) key_nx = (unsigned)(__ldg(a.keys + rs + 1) & 0xffffffffull);
+            const float4 *cA = recA + kap;                                      // this lane's slots
+            const float4 *cT = reinterpret_cast<const float4 *>(recT) + gr;
             for (int64_t j = rs; j < re; ++j) {
                 const uint2 m = m_nx;
                 const float4 d = d_nx;
@@ -813,28 +819,34 @@ __global__ void __launch_bounds__(NWT * 32, 1) k_tiles(const TileArgs a) {
                     fetch(key_nx);
                     if (j + 2 < re) key_nx = (unsigned)(__ldg(a.keys + j + 2) & 0xffffffffull);
                 }
-                // ---- producer: lane = step ----
+                // ---- producer: lane = step, records in residue-class order ----
                 {
                     float4 *ra = recA + lane * SUP;
-                    float *rv = recV + lane * REC_V;
+                    float2 *rt = recT + lane * RT;
                     if (m.x != NO_CELL) {
+                        const int cu = (int)(m.x >> 16), cv = (int)(m.x & 0xffffu);
                         const int ou = (int)(m.y & 0xffffu) - 32768, ov = (int)(m.y >> 16) - 32768;
+                        int ku = (int)((unsigned)(cu - SC) % 7u), kv = (int)((unsigned)(cv - SC) % 7u);
 #pragma unroll
                         for (int k = 0; k < SUP; ++k) {
                             const float tu = tab[abs(os * (k - SC) + ou)];
+                            const float tv = tab[abs(os * (k - SC) + ov)];
                             const float2 t2 = make_float2(tu, tu);
                             const float2 lo = __fmul2_rn(t2, make_float2(d.x, d.y));
                             const float2 hi = __fmul2_rn(t2, make_float2(d.z, d.w));
-                            ra[k] = make_float4(lo.x, lo.y, hi.x, hi.y);
-                            rv[k] = tab[abs(os * (k - SC) + ov)];
+                            ra[ku] = make_float4(lo.x, lo.y, hi.x, hi.y);
+                            rt[kv] = make_float2(tv, tv);
+                            ku = ku == 6 ? 0 : ku + 1;
+                            kv = kv == 6 ? 0 : kv + 1;
                         }
                     } else {
 #pragma unroll
                         for (int k = 0; k < SUP; ++k) {
                             ra[k] = make_float4(0.f, 0.f, 0.f, 0.f);
-                            rv[k] = 0.f;
+                            rt[k] = make_float2(0.f, 0.f);
                         }
                     }
+                    rt[SUP] = make_float2(0.f, 0.f);   // v class 7 does not exist (second row of g = 3)
                     recC[lane] = m.x;
                 }
                 __syncwarp();
@@ -843,14 +855,13 @@ __global__ void __launch_bounds__(NWT * 32, 1) k_tiles(const TileArgs a) {
                 for (int s = 0; s < CH; ++s) {
                     const unsigned cuv = recC[s];
                     if (cuv != cur && cuv != NO_CELL) change(cuv);
-                    const float4 A = recA[s * SUP + kA];
-                    const float t0 = recV[s * REC_V + kV0], t1 = recV[s * REC_V + kV1];
-                    const float2 T0 = make_float2(t0, t0), T1 = make_float2(t1, t1);
-                    acc[0][0] = __ffma2_rn(make_float2(A.x, A.y), T0, acc[0][0]);
-                    acc[1][0] = __ffma2_rn(make_float2(A.x, A.y), T1, acc[1][0]);
+                    const float4 A = cA[s * SUP];
+                    const float4 T = cT[s * (RT / 2)];   // (t0, t0, t1, t1): this lane's two v taps
+                    acc[0][0] = __ffma2_rn(make_float2(A.x, A.y), make_float2(T.x, T.y), acc[0][0]);
+                    acc[1][0] = __ffma2_rn(make_float2(A.x, A.y), make_float2(T.z, T.w), acc[1][0]);
                     if constexpr (CPLX && NP > 1) {
-                        acc[0][1] = __ffma2_rn(make_float2(A.z, A.w), T0, acc[0][1]);
-                        acc[1][1] = __ffma2_rn(make_float2(A.z, A.w), T1, acc[1][1]);
+                        acc[0][1] = __ffma2_rn(make_float2(A.z, A.w), make_float2(T.x, T.y), acc[0][1]);
+                        acc[1][1] = __ffma2_rn(make_float2(A.z, A.w), make_float2(T.z, T.w), acc[1][1]);
                     }
                 }
                 // bound the register sums to one chunk (32 steps)
@@ -1303,10 +1314,21 @@ int grid_ps_impl(const NggGridArgs *a, int64_t c_off, int64_t c_stride, const Ng
             pa.n_img = n_img;
             pa.continuum = a->chan_mode == NGG_CHAN_CONTINUUM;
             const dim3 pg((unsigned)B, (unsigned)nk, (unsigned)((C + 31) / 32)), pb(32, 8);
+            // the imaging-weight / flag variant only where it is asked for (its
+            // extra registers cost the plain pass a third of its speed)
+            const bool fused = pa.density != nullptr || pa.flag != nullptr;
             if (np == 2) {
-                if (cplx) k_pack<2, true><<<pg, pb, 0, s>>>(pa); else k_pack<2, false><<<pg, pb, 0, s>>>(pa);
+                if (cplx) {
+                    if (fused) k_pack<2, true, true><<<pg, pb, 0, s>>>(pa); else k_pack<2, true, false><<<pg, pb, 0, s>>>(pa);
+                } else {
+                    if (fused) k_pack<2, false, true><<<pg, pb, 0, s>>>(pa); else k_pack<2, false, false><<<pg, pb, 0, s>>>(pa);
+                }
             } else {
-                if (cplx) k_pack<1, true><<<pg, pb, 0, s>>>(pa); else k_pack<1, false><<<pg, pb, 0, s>>>(pa);
+                if (cplx) {
+                    if (fused) k_pack<1, true, true><<<pg, pb, 0, s>>>(pa); else k_pack<1, true, false><<<pg, pb, 0, s>>>(pa);
+                } else {
+                    if (fused) k_pack<1, false, true><<<pg, pb, 0, s>>>(pa); else k_pack<1, false, false><<<pg, pb, 0, s>>>(pa);
+                }
             }
             NGG_CHECK_LAUNCH("k_pack");
             k_sw_reduce<<<(unsigned)(n_img * np), 256, 0, s>>>(sw_part, C, np, B * nk, ta.continuum, P, (int)p0,

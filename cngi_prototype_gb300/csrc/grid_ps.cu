@@ -187,7 +187,7 @@ __device__ __forceinline__ bool step_imaging_weights(const PackArgs &a, float4 u
 // channels x 32 steps of one (baseline, chunk): the reads are contiguous over
 // channels, a shared-memory transpose makes the writes contiguous over time.
 template <int NP, bool CPLX, bool FUSED>
-__global__ void __launch_bounds__(256) k_pack(const PackArgs a) {
+__global__ void __launch_bounds__(256, 4) k_pack(const PackArgs a) {
     __shared__ uint2 s_meta[32][33];
     __shared__ float4 s_wv[32][33];
     __shared__ float s_sw[NP][32][9];       // per channel: the 8 row-threads' partial sums
@@ -202,68 +202,96 @@ __global__ void __launch_bounds__(256) k_pack(const PackArgs a) {
     float swc[NP];   // this thread's sum_weight terms over its 4 steps
 #pragma unroll
     for (int p = 0; p < NP; ++p) swc[p] = 0.f;
-    for (int y = threadIdx.y; y < 32; y += 8) {
-        const int64_t c = c0 + x, t = (int64_t)k * CH + y;
+    // All loads of the thread's 4 steps are issued before any index
+    // arithmetic, so the pass waits for memory once rather than twice per
+    // step (uvw and channel scale, then visibilities and weights).
+    const int64_t c = c0 + x;
+    const bool c_ok = c < a.C;
+    ChanParms cp{};
+    if (c_ok) cp = a.chan[c];
+    float4 us4[4];
+    float wl[4][NP];
+    float2 vl[4][NP];
+#pragma unroll
+    for (int i = 0; i < 4; ++i) {
+        const int64_t t = (int64_t)k * CH + threadIdx.y + 8 * i;
+        us4[i] = make_float4(NAN, 0.f, NAN, 0.f);
+#pragma unroll
+        for (int p = 0; p < NP; ++p) {
+            wl[i][p] = 0.f;
+            vl[i][p] = make_float2(0.f, 0.f);
+        }
+        if (c_ok && t < a.T) {
+            us4[i] = a.uvs[b * a.T + t];
+            const int64_t base = ((t * a.B + b) * a.c_stride + a.c_off + c) * a.P + a.p0;
+#pragma unroll
+            for (int p = 0; p < NP; ++p) {
+                if (!FUSED) wl[i][p] = a.weight[base + p];
+                if constexpr (CPLX) vl[i][p] = a.vis[base + p];
+            }
+        }
+    }
+#pragma unroll
+    for (int i = 0; i < 4; ++i) {
+        const int y = threadIdx.y + 8 * i;
+        const int64_t t = (int64_t)k * CH + y;
         uint2 meta = make_uint2(NO_CELL, 0u);
         float4 wv = make_float4(0.f, 0.f, 0.f, 0.f);
-        if (c < a.C && t < a.T) {
-            const float4 us = a.uvs[b * a.T + t];
-            if (!isnan(us.x) && !isnan(us.z)) {
-                const ChanParms cp = a.chan[c];
-                int cu, ou, cv, ov;
-                if (!cell_pair(us.x, us.y, cp.suh, cp.sul, false, cu_c, a.os, cu, ou)) {
-                    long long i64, o64;
-                    cell_fp64(a.uvw[(t * a.B + b) * 3 + 0], cp.su, false, cu_c, a.os, i64, o64);
-                    cu = (int)max(min(i64, (long long)1 << 30), -((long long)1 << 30));
-                    ou = (int)o64;
-                }
-                if (!cell_pair(us.z, us.w, cp.svh, cp.svl, false, cv_c, a.os, cv, ov)) {
-                    long long i64, o64;
-                    cell_fp64(a.uvw[(t * a.B + b) * 3 + 1], cp.sv, false, cv_c, a.os, i64, o64);
-                    cv = (int)max(min(i64, (long long)1 << 30), -((long long)1 << 30));
-                    ov = (int)o64;
-                }
-                if (cu - SC >= 0 && cu + SC < a.nu && cv - SC >= 0 && cv + SC < a.nv) {
-                    const int64_t base = ((t * a.B + b) * a.c_stride + a.c_off + c) * a.P + a.p0;
-                    float w[NP];
-                    bool pv[NP];
-                    bool any = false;
-                    bool in_density = true;
-                    if constexpr (FUSED) {
-                        if (a.density) in_density = step_imaging_weights<NP>(a, us, t, b, c, base, w);
-                        else {
-#pragma unroll
-                            for (int p = 0; p < NP; ++p) w[p] = a.weight[base + p];
-                        }
-                    } else {
+        const float4 us = us4[i];
+        if (c_ok && t < a.T && !isnan(us.x) && !isnan(us.z)) {
+            int cu, ou, cv, ov;
+            if (!cell_pair(us.x, us.y, cp.suh, cp.sul, false, cu_c, a.os, cu, ou)) {
+                long long i64, o64;
+                cell_fp64(a.uvw[(t * a.B + b) * 3 + 0], cp.su, false, cu_c, a.os, i64, o64);
+                cu = (int)max(min(i64, (long long)1 << 30), -((long long)1 << 30));
+                ou = (int)o64;
+            }
+            if (!cell_pair(us.z, us.w, cp.svh, cp.svl, false, cv_c, a.os, cv, ov)) {
+                long long i64, o64;
+                cell_fp64(a.uvw[(t * a.B + b) * 3 + 1], cp.sv, false, cv_c, a.os, i64, o64);
+                cv = (int)max(min(i64, (long long)1 << 30), -((long long)1 << 30));
+                ov = (int)o64;
+            }
+            if (cu - SC >= 0 && cu + SC < a.nu && cv - SC >= 0 && cv + SC < a.nv) {
+                const int64_t base = ((t * a.B + b) * a.c_stride + a.c_off + c) * a.P + a.p0;
+                float w[NP];
+                bool pv[NP];
+                bool any = false;
+                bool in_density = true;
+                if constexpr (FUSED) {
+                    if (a.density) in_density = step_imaging_weights<NP>(a, us, t, b, c, base, w);
+                    else {
 #pragma unroll
                         for (int p = 0; p < NP; ++p) w[p] = a.weight[base + p];
                     }
+                } else {
 #pragma unroll
-                    for (int p = 0; p < NP; ++p) {
-                        if (!in_density) w[p] = 0.f;
-                        if constexpr (CPLX) {
-                            const float2 vv = a.vis[base + p];
-                            const float xr = vv.x * w[p], xi = vv.y * w[p];
-                            pv[p] = !isnan(xr) && !isnan(xi) && (xr != 0.f || xi != 0.f);
-                            if (FUSED && a.flag && a.flag[base + p]) pv[p] = false;   // flagged: the visibility is NaN
-                            if (p == 0) { wv.x = pv[p] ? xr : 0.f; wv.y = pv[p] ? xi : 0.f; }
-                            else { wv.z = pv[p] ? xr : 0.f; wv.w = pv[p] ? xi : 0.f; }
-                        } else {
-                            pv[p] = !isnan(w[p]) && w[p] != 0.f;
-                            if (p == 0) wv.x = pv[p] ? w[p] : 0.f;
-                            else wv.y = pv[p] ? w[p] : 0.f;
-                        }
-                        any = any || pv[p];
-                    }
-                    if (any) {
-                        meta = make_uint2(((unsigned)cu << 16) | (unsigned)cv,
-                                          (unsigned)(ou + 32768) | ((unsigned)(ov + 32768) << 16));
-                        const float norm = s_nsum[ou + a.os / 2] * s_nsum[ov + a.os / 2];
+                    for (int p = 0; p < NP; ++p) w[p] = wl[i][p];
+                }
 #pragma unroll
-                        for (int p = 0; p < NP; ++p)
-                            if (pv[p]) swc[p] = __fadd_rn(swc[p], __fmul_rn(w[p], norm));
+                for (int p = 0; p < NP; ++p) {
+                    if (!in_density) w[p] = 0.f;
+                    if constexpr (CPLX) {
+                        const float2 vv = vl[i][p];
+                        const float xr = vv.x * w[p], xi = vv.y * w[p];
+                        pv[p] = !isnan(xr) && !isnan(xi) && (xr != 0.f || xi != 0.f);
+                        if (FUSED && a.flag && a.flag[base + p]) pv[p] = false;   // flagged: the visibility is NaN
+                        if (p == 0) { wv.x = pv[p] ? xr : 0.f; wv.y = pv[p] ? xi : 0.f; }
+                        else { wv.z = pv[p] ? xr : 0.f; wv.w = pv[p] ? xi : 0.f; }
+                    } else {
+                        pv[p] = !isnan(w[p]) && w[p] != 0.f;
+                        if (p == 0) wv.x = pv[p] ? w[p] : 0.f;
+                        else wv.y = pv[p] ? w[p] : 0.f;
                     }
+                    any = any || pv[p];
+                }
+                if (any) {
+                    meta = make_uint2(((unsigned)cu << 16) | (unsigned)cv,
+                                      (unsigned)(ou + 32768) | ((unsigned)(ov + 32768) << 16));
+                    const float norm = s_nsum[ou + a.os / 2] * s_nsum[ov + a.os / 2];
+#pragma unroll
+                    for (int p = 0; p < NP; ++p)
+                        if (pv[p]) swc[p] = __fadd_rn(swc[p], __fmul_rn(w[p], norm));
                 }
             }
         }

@@ -66,7 +66,11 @@ def test_auto_fft_precision_is_double_for_small_cubes(ngg):
     auto = make_image(mx, xds.Dataset(), _gp(d), {'xds': 'xds0'}, {})['IMAGE'].values
     double = make_image(mx, xds.Dataset(), dict(_gp(d), fft_precision='double'), {'xds': 'xds0'},
                         {})['IMAGE'].values
-    assert np.abs(auto - double).max() <= 1e-6 * np.abs(double).max()   # gridding atomics vary in FP32 rounding
+    # two gridding runs: the FP32 shared-memory atomics of the tile pass land
+    # in a different order each run, and the correction image (1.3e-3 in the
+    # corners) amplifies that rounding difference ~770x; both runs are
+    # within 1e-5 of the reference (test_make_image_and_psf)
+    assert np.abs(auto - double).max() <= 2e-6 * np.abs(double).max()
     assert fft_precision({}, 256, 2, (4915, 4915)) == 'single'
     assert fft_precision({}, 32, 2, (614, 614)) == 'double'
     assert fft_precision({'fft_precision': 'single'}, 1, 1, (8, 8)) == 'single'

@@ -129,4 +129,7 @@ def test_make_image_from_a_store_equals_make_image_in_memory(ngg, tmp_path):
     a = make_image(m, xds.Dataset(), gp, {'xds': 'xds0'}, {})['IMAGE'].values
     b = make_image(r, xds.Dataset(), gp, {'xds': 'xds0'}, {})['IMAGE'].values
     assert a.shape == b.shape
-    assert np.abs(a - b).max() <= 1e-6 * np.abs(a).max()
+    # the tile pass's FP32 shared-memory atomics land in a different order
+    # each run; the correction image (1.3e-3 in the corners) amplifies that
+    # rounding difference ~770x, to ~1e-6 of the peak
+    assert np.abs(a - b).max() <= 2e-6 * np.abs(a).max()

@@ -40,7 +40,6 @@
 #include <cub/cub.cuh>
 
 #include <algorithm>
-#include <mutex>
 #include <vector>
 
 #include "ngg_internal.cuh"
@@ -564,64 +563,75 @@ __global__ void k_zero_split(const int64_t *bin_start, const int *bbox, int n_im
     }
 }
 
-// Zero the cells in [p0, p1) (cells of elem bytes, p0 a multiple of elem):
-// the warp's lanes store 16-byte runs of zeros where the address is 16-byte
-// aligned and single cells at the two ragged ends.
-__device__ __forceinline__ void warp_zero(char *p0, char *p1, int elem, int lane) {
-    if (p1 <= p0) return;
-    const uintptr_t mis = (uintptr_t)p0 & 15;
-    char *ah = mis ? p0 + (16 - mis) : p0;
-    if (ah > p1) ah = p1;
-    for (char *q = p0 + lane * elem; q < ah; q += 32 * elem) {
+constexpr int ZBUF = 2048;   // bytes of zeros in shared memory: the source of the zero-fill bulk stores
+
+// Zero nbytes of the grid at gp (gp and nbytes multiples of elem): plain
+// stores up to the first 16-byte boundary and after the last one, TMA bulk
+// stores (asynchronous; committed by the caller) from the zero buffer at
+// shared address zs for the aligned middle.
+__device__ __forceinline__ void zero_fill(char *gp, int64_t nbytes, unsigned zs, int elem) {
+    while (nbytes > 0 && ((uintptr_t)gp & 15)) {
+        if (elem == 8) *reinterpret_cast<float2 *>(gp) = make_float2(0.f, 0.f);
+        else *reinterpret_cast<float *>(gp) = 0.f;
+        gp += elem;
+        nbytes -= elem;
+    }
+    const int64_t mid = nbytes & ~(int64_t)15;
+    for (char *q = gp + mid; q < gp + nbytes; q += elem) {
         if (elem == 8) *reinterpret_cast<float2 *>(q) = make_float2(0.f, 0.f);
         else *reinterpret_cast<float *>(q) = 0.f;
     }
-    char *tail = ah + ((p1 - ah) & ~(ptrdiff_t)15);
-    for (char *q = ah + lane * 16; q < tail; q += 32 * 16) *reinterpret_cast<float4 *>(q) = make_float4(0.f, 0.f, 0.f, 0.f);
-    for (char *q = tail + lane * elem; q < p1; q += 32 * elem) {
-        if (elem == 8) *reinterpret_cast<float2 *>(q) = make_float2(0.f, 0.f);
-        else *reinterpret_cast<float *>(q) = 0.f;
+    for (int64_t o = 0; o < mid; o += ZBUF) {
+        const unsigned sz = (unsigned)(mid - o < ZBUF ? mid - o : ZBUF);
+        asm volatile("cp.async.bulk.global.shared::cta.bulk_group [%0], [%1], %2;" ::"l"(gp + o), "r"(zs), "r"(sz)
+                     : "memory");
     }
 }
 
-// Every cell outside the busy box, in every plane of the call: the tile kernel
-// writes all the box's tiles, so this is the rest of the grid -- whole rows
-// outside the box's u range, and in the rows inside it the columns outside
-// its v range (in stored order: FFT-layout planes are ifftshift-ed). It runs
-// on a side stream from the end of binning on, with a few small CTAs per SM
-// that fit beside the packing and tile kernels, so the zeros (94 GB for the
-// large cube) go out while the SMs pack and grid instead of after them.
-constexpr int ZERO_THREADS = 64;
-__global__ void __launch_bounds__(ZERO_THREADS) k_zero_outside(void *grid, int elem, const int *bbox, int n_img,
-                                                              int64_t NT, int ntv, int64_t planes, int64_t nu,
-                                                              int64_t nv, int fftl) {
-    const BoxMap m = box_map(bbox, n_img, NT, ntv);
-    const int R0 = m.nbu ? m.bt0 * TU : 0, R1 = m.nbu ? min((m.bt0 + m.nbu) * TU, (int)nu) : 0;
-    const int V0 = m.nbv ? m.bv0 * TV : 0, V1 = m.nbv ? min((m.bv0 + m.nbv) * TV, (int)nv) : 0;
-    const int cu_c = (int)(nu / 2), cv_c = (int)(nv / 2);
-    const int lane = threadIdx.x & 31;
-    const int64_t warps = (int64_t)gridDim.x * (ZERO_THREADS / 32);
-    const int64_t n_rows = planes * nu;
-    for (int64_t row = (int64_t)blockIdx.x * (ZERO_THREADS / 32) + threadIdx.x / 32; row < n_rows; row += warps) {
-        const int r = (int)(row % nu);
-        const int un = fftl ? (r + cu_c >= nu ? r + cu_c - (int)nu : r + cu_c) : r;   // natural row
-        char *base = reinterpret_cast<char *>(grid) + row * nv * elem;
-        if (!(un >= R0 && un < R1 && V1 > V0)) {
-            warp_zero(base, base + nv * elem, elem, lane);
+struct ZeroRows {
+    void *grid;
+    int64_t nu, nv, P;
+    int p0, nrb;
+    int64_t n_items;
+    int R0, R1, V0, V1, cu_c, cv_c;   // busy box rows/columns (natural order), grid centre
+    unsigned zs;                       // shared address of the zero buffer
+    int *counter;
+};
+
+// Take the next block of ZR rows outside the busy box and zero it (the part
+// of each row outside the box, in stored order); false when none is left.
+template <int NP, int ELEM, bool FFTL>
+__device__ __noinline__ bool zero_next(const ZeroRows &z) {
+    constexpr int ZR = 8;
+    const long long it = atomicAdd(z.counter, 1);
+    if (it >= z.n_items) return false;
+    const int64_t q = it / z.nrb;
+    const int rb = (int)(it % z.nrb);
+    const int cimg = (int)(q / NP), p = (int)(q % NP);
+    const int64_t pbase = ((int64_t)cimg * z.P + z.p0 + p) * z.nu * z.nv;
+    const int r_end = min(rb * ZR + ZR, (int)z.nu);
+    for (int r = rb * ZR; r < r_end; ++r) {
+        const int un = FFTL ? (r + z.cu_c >= z.nu ? r + z.cu_c - (int)z.nu : r + z.cu_c) : r;   // natural row
+        char *row = reinterpret_cast<char *>(z.grid) + (pbase + (int64_t)r * z.nv) * ELEM;
+        if (!(un >= z.R0 && un < z.R1 && z.V1 > z.V0)) {
+            zero_fill(row, z.nv * ELEM, z.zs, ELEM);
             continue;
         }
         // stored columns of the natural busy range [V0, V1)
-        int s0 = V0;
-        const int L = V1 - V0;
-        if (fftl) { s0 = V0 - cv_c; if (s0 < 0) s0 += (int)nv; }
-        if (s0 + L <= nv) {
-            warp_zero(base, base + (int64_t)s0 * elem, elem, lane);
-            warp_zero(base + (int64_t)(s0 + L) * elem, base + nv * elem, elem, lane);
+        int s0 = z.V0;
+        const int L = z.V1 - z.V0;
+        if (FFTL) { s0 = z.V0 - z.cv_c; if (s0 < 0) s0 += (int)z.nv; }
+        if (s0 + L <= z.nv) {
+            zero_fill(row, (int64_t)s0 * ELEM, z.zs, ELEM);
+            zero_fill(row + (int64_t)(s0 + L) * ELEM, (z.nv - s0 - L) * ELEM, z.zs, ELEM);
         } else {
-            const int e = s0 + L - (int)nv;
-            warp_zero(base + (int64_t)e * elem, base + (int64_t)s0 * elem, elem, lane);
+            const int e = s0 + L - (int)z.nv;
+            zero_fill(row + (int64_t)e * ELEM, (int64_t)(s0 - e) * ELEM, z.zs, ELEM);
         }
     }
+    asm volatile("cp.async.bulk.commit_group;" ::: "memory");
+    asm volatile("cp.async.bulk.wait_group.read 32;" ::: "memory");   // bound the stores in flight
+    return true;
 }
 
 // ---- the tile kernel: one track per warp ------------------------------------
@@ -677,6 +687,8 @@ __global__ void __launch_bounds__(NWT * 32, 1) k_tiles(const TileArgs a) {
     unsigned char *recs = reinterpret_cast<unsigned char *>(tab + ((a.tab_bytes + 3) / 4));
     unsigned long long *mbar = reinterpret_cast<unsigned long long *>(recs + (size_t)NWT * WARP_REC_BYTES);
     int *s_item = reinterpret_cast<int *>(mbar + 1);   // [kind, item]
+    float4 *zbuf = reinterpret_cast<float4 *>(
+        (reinterpret_cast<uintptr_t>(s_item + 2) + 15) & ~static_cast<uintptr_t>(15));
 
     const int tid = threadIdx.x;
     const int warp = tid >> 5, lane = tid & 31;
@@ -708,7 +720,10 @@ __global__ void __launch_bounds__(NWT * 32, 1) k_tiles(const TileArgs a) {
         return;
     }
     for (int i = tid; i < NPL * TU * TV; i += blockDim.x) acc_s[i] = 0.f;
+    for (int i = tid; i < ZBUF / 16; i += blockDim.x) zbuf[i] = make_float4(0.f, 0.f, 0.f, 0.f);
+    asm volatile("fence.proxy.async.shared::cta;" ::: "memory");   // the bulk stores read zbuf
     __syncthreads();
+    const unsigned zs = (unsigned)__cvta_generic_to_shared(zbuf);
 
     float4 *recA = reinterpret_cast<float4 *>(recs + (size_t)warp * WARP_REC_BYTES);   // [CH][SUP] by u class
     float2 *recT = reinterpret_cast<float2 *>(recA + CH * SUP);                         // [CH][RT] by v class
@@ -718,7 +733,12 @@ __global__ void __launch_bounds__(NWT * 32, 1) k_tiles(const TileArgs a) {
     const int cu_c = (int)(a.nu / 2), cv_c = (int)(a.nv / 2);
     const int64_t plane = a.nu * a.nv;
     const BoxMap bm = box_map(a.bbox, a.n_img, NT, a.ntv);
+    const int R0 = bm.nbu ? bm.bt0 * TU : 0, R1 = bm.nbu ? min((bm.bt0 + bm.nbu) * TU, (int)a.nu) : 0;
+    const int V0 = bm.nbv ? bm.bv0 * TV : 0, V1 = bm.nbv ? min((bm.bv0 + bm.nbv) * TV, (int)a.nv) : 0;
     const int64_t n_tile_items = *a.n_subs;
+    constexpr int ZR = 8;
+    const int nrb = (int)((a.nu + ZR - 1) / ZR);
+    const int64_t n_zero_items = (int64_t)a.n_img * NP * nrb;
     const int os = a.os;
 
     // this lane's residue classes (consumer)
@@ -728,6 +748,13 @@ __global__ void __launch_bounds__(NWT * 32, 1) k_tiles(const TileArgs a) {
     const bool has1 = act && g < 3;
     const int gr = g < 3 ? g : 3;   // lanes 28-31 read a valid slot (and never flush)
 
+    // Rows outside the busy box are zeroed by TMA bulk stores that lane 0 of
+    // each warp issues, one block of rows at a time, just before the warp
+    // waits at a tile barrier (the rest after the last tile): the grid write
+    // they carry overlaps the tile work instead of taking CTAs away from it.
+    const ZeroRows zr{a.grid, a.nu, a.nv, a.P, a.p0, nrb, n_zero_items, R0, R1, V0, V1, cu_c, cv_c, zs,
+                      &a.work_counter[1]};
+    bool zero_left = lane == 0;
     for (;;) {
         if (tid == 0) {
             const long long it = atomicAdd(&a.work_counter[0], 1);
@@ -869,6 +896,7 @@ __global__ void __launch_bounds__(NWT * 32, 1) k_tiles(const TileArgs a) {
                 flush(0); zero(0); flush(1); zero(1);
                 __syncwarp();   // the producer of the next chunk overwrites the records
             }
+            if (zero_left) zero_left = zero_next<NP, (CPLX || FFTL) ? 8 : 4, FFTL>(zr);
             __syncthreads();   // every warp's cells are in the tile
         }
 
@@ -917,7 +945,12 @@ __global__ void __launch_bounds__(NWT * 32, 1) k_tiles(const TileArgs a) {
                 }
             }
         }
+        if (zero_left) zero_left = zero_next<NP, (CPLX || FFTL) ? 8 : 4, FFTL>(zr);
         __syncthreads();
+    }
+    if (lane == 0) {
+        while (zero_left) zero_left = zero_next<NP, (CPLX || FFTL) ? 8 : 4, FFTL>(zr);
+        asm volatile("cp.async.bulk.wait_group 0;" ::: "memory");   // the zero rows are written
     }
 }
 
@@ -925,7 +958,7 @@ size_t tile_smem_bytes(int np, bool cplx, int tab_bytes) {
     const size_t acc = (size_t)(cplx ? 2 * np : np) * TU * TV * 4;
     const size_t tab = (size_t)((tab_bytes + 3) / 4) * 4;
     const size_t rec = (size_t)NWT * WARP_REC_BYTES;
-    return acc + tab + rec + 8 + 8 + 16;
+    return acc + tab + rec + 8 + 8 + 16 + ZBUF;
 }
 
 template <int NP, bool CPLX, bool FFTL>
@@ -994,35 +1027,6 @@ __global__ void k_table(const double *cgk, int n, int npad, float *tab) {
 }
 
 }  // namespace
-
-// The side stream on which the zero fill outside the busy box runs, one per
-// device (created on first use, kept for the life of the process), and the
-// pair of events that orders it after the call's binning and before the
-// call's end on the caller's stream. The guard's destructor makes the
-// caller's stream wait for the fill on every exit path, so the grid is
-// complete whenever the call's work on that stream is.
-cudaStream_t side_stream(int dev) {
-    static std::mutex mu;
-    static cudaStream_t st[64] = {};
-    std::lock_guard<std::mutex> lk(mu);
-    if (dev < 0 || dev >= 64) return nullptr;
-    if (!st[dev] && cudaStreamCreateWithFlags(&st[dev], cudaStreamNonBlocking) != cudaSuccess) {
-        cudaGetLastError();
-        st[dev] = nullptr;
-    }
-    return st[dev];
-}
-
-struct SideFill {
-    cudaStream_t main = nullptr, side = nullptr;
-    cudaEvent_t start = nullptr, done = nullptr;
-    bool launched = false;
-    ~SideFill() {
-        if (launched) cudaStreamWaitEvent(main, done, 0);
-        if (start) cudaEventDestroy(start);
-        if (done) cudaEventDestroy(done);
-    }
-};
 
 struct Scratch {
     std::vector<void *> ptrs;
@@ -1237,26 +1241,6 @@ int grid_ps_impl(const NggGridArgs *a, int64_t c_off, int64_t c_stride, const Ng
     k_bbox_init<<<1, 1, 0, s>>>(bbox_d);
     k_bbox<<<(unsigned)((n_bins + 255) / 256), 256, 0, s>>>(bin_start, n_bins, (int64_t)ntu * ntv, ntv, bbox_d);
     NGG_CHECK_LAUNCH("k_bbox");
-    // the zero fill outside the busy box, on the side stream from here on
-    // (it overlaps the packing and tile passes; its cells are disjoint from
-    // every cell they write)
-    SideFill fill;
-    {
-        int dev = 0;
-        NGG_CUDA(cudaGetDevice(&dev));
-        fill.main = s;
-        fill.side = side_stream(dev);
-        if (!fill.side) return fail(NGG_ERR_CUDA, "could not create the zero-fill side stream");
-        NGG_CUDA(cudaEventCreateWithFlags(&fill.start, cudaEventDisableTiming));
-        NGG_CUDA(cudaEventCreateWithFlags(&fill.done, cudaEventDisableTiming));
-        NGG_CUDA(cudaEventRecord(fill.start, s));
-        NGG_CUDA(cudaStreamWaitEvent(fill.side, fill.start, 0));
-        k_zero_outside<<<(unsigned)(2 * num_sms()), ZERO_THREADS, 0, fill.side>>>(
-            a->grid, (int)elem, bbox_d, n_img, (int64_t)ntu * ntv, ntv, (int64_t)n_img * P, nu, nv, fftl ? 1 : 0);
-        NGG_CHECK_LAUNCH("k_zero_outside");
-        NGG_CUDA(cudaEventRecord(fill.done, fill.side));
-        fill.launched = true;
-    }
     // tile work items: every (tile in the busy box, channel); bins with more
     // than MAXE entries become several items
     const int64_t n_bound = n_bins;   // box items <= bins
@@ -1328,6 +1312,7 @@ int grid_ps_impl(const NggGridArgs *a, int64_t c_off, int64_t c_stride, const Ng
     ta.subs = subs;
     ta.n_subs = n_subs_d;
     ta.bnk = (unsigned)(B * nk);
+    (void)elem;
     for (int64_t p0 = 0, launch = 0; p0 < P; ++launch) {
         const int np = (P - p0) >= 2 ? 2 : 1;
         ta.p0 = (int)p0;
@@ -1386,7 +1371,6 @@ int grid_ps_impl(const NggGridArgs *a, int64_t c_off, int64_t c_stride, const Ng
         p0 += np;
         if (launch >= 62) return fail(NGG_ERR_UNSUPPORTED, "too many polarizations");
     }
-    NGG_CUDA(cudaStreamWaitEvent(s, fill.done, 0));   // the grid is whole from here on the caller's stream
     prof_record(2, s);
     // the tile kernel's bounded wait for its table copy: report a time-out
     int err = 0;

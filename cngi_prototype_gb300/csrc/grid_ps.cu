@@ -630,7 +630,7 @@ __device__ __noinline__ bool zero_next(const ZeroRows &z) {
         }
     }
     asm volatile("cp.async.bulk.commit_group;" ::: "memory");
-    asm volatile("cp.async.bulk.wait_group.read 32;" ::: "memory");   // bound the stores in flight
+    asm volatile("cp.async.bulk.wait_group.read 4;" ::: "memory");   // bound this thread's stores in flight
     return true;
 }
 
@@ -666,6 +666,9 @@ constexpr int NWT = 24;                  // warps per CTA (one CTA per SM)
 constexpr int RT = 10;                   // float2 per step of v-tap pairs (16-byte rows; 8 used)
 constexpr int WARP_REC_BYTES = CH * SUP * 16 + CH * RT * 8 + CH * 4;
 
+// the tile kernel's compute warps (all but the zero-fill warp)
+__device__ __forceinline__ void compute_sync() { asm volatile("bar.sync 1, %0;" ::"n"(NWT * 32) : "memory"); }
+
 __device__ __forceinline__ int tile_addr(int lu, int lv) { return lu * TV + (lv ^ ((lu & 7) << 2)); }
 
 __device__ __forceinline__ void red_shared(float *p, float v) {
@@ -678,7 +681,7 @@ __device__ __forceinline__ int residue_cell(int lo, int cls) {
 }
 
 template <int NP, bool CPLX, bool FFTL>
-__global__ void __launch_bounds__(NWT * 32, 1) k_tiles(const TileArgs a) {
+__global__ void __launch_bounds__((NWT + 1) * 32, 1) k_tiles(const TileArgs a) {
     extern __shared__ __align__(16) unsigned char smem[];
     constexpr int NPL = CPLX ? 2 * NP : NP;   // float planes of the tile
     constexpr int NA = CPLX ? NP : 1;         // float2 accumulators per cell
@@ -748,20 +751,27 @@ __global__ void __launch_bounds__(NWT * 32, 1) k_tiles(const TileArgs a) {
     const bool has1 = act && g < 3;
     const int gr = g < 3 ? g : 3;   // lanes 28-31 read a valid slot (and never flush)
 
-    // Rows outside the busy box are zeroed by TMA bulk stores that lane 0 of
-    // each warp issues, one block of rows at a time, just before the warp
-    // waits at a tile barrier (the rest after the last tile): the grid write
-    // they carry overlaps the tile work instead of taking CTAs away from it.
+    // Warp NWT zeroes the rows outside the busy box: each of its lanes takes
+    // blocks of rows from a counter and zeroes them with TMA bulk stores from
+    // the shared zero buffer, independently of the tile work (the compute
+    // warps synchronise on a named barrier of their own), so the grid's
+    // zeros stream out while the other warps grid.
     const ZeroRows zr{a.grid, a.nu, a.nv, a.P, a.p0, nrb, n_zero_items, R0, R1, V0, V1, cu_c, cv_c, zs,
                       &a.work_counter[1]};
-    bool zero_left = lane == 0;
+    if (warp == NWT) {
+        while (zero_next<NP, (CPLX || FFTL) ? 8 : 4, FFTL>(zr)) {
+        }
+        asm volatile("cp.async.bulk.wait_group 0;" ::: "memory");   // this lane's zero rows are written
+        return;
+    }
+    constexpr int NCT = NWT * 32;   // compute threads
     for (;;) {
         if (tid == 0) {
             const long long it = atomicAdd(&a.work_counter[0], 1);
             s_item[0] = it < n_tile_items ? 0 : -1;
             s_item[1] = (int)it;
         }
-        __syncthreads();
+        compute_sync();
         const int kind = s_item[0];
         const int64_t item = s_item[1];
         if (kind < 0) break;
@@ -896,14 +906,13 @@ __global__ void __launch_bounds__(NWT * 32, 1) k_tiles(const TileArgs a) {
                 flush(0); zero(0); flush(1); zero(1);
                 __syncwarp();   // the producer of the next chunk overwrites the records
             }
-            if (zero_left) zero_left = zero_next<NP, (CPLX || FFTL) ? 8 : 4, FFTL>(zr);
-            __syncthreads();   // every warp's cells are in the tile
+            compute_sync();   // every warp's cells are in the tile
         }
 
         // ---------------- write the tile ----------------
         const bool busy = e0 < e1;
         if (!(split && !busy)) {
-            for (int e = tid; e < NP * TU * TV; e += blockDim.x) {
+            for (int e = tid; e < NP * TU * TV; e += NCT) {
                 const int p = e / (TU * TV);
                 const int r = (e / TV) % TU;
                 const int cl = e % TV;
@@ -945,12 +954,7 @@ __global__ void __launch_bounds__(NWT * 32, 1) k_tiles(const TileArgs a) {
                 }
             }
         }
-        if (zero_left) zero_left = zero_next<NP, (CPLX || FFTL) ? 8 : 4, FFTL>(zr);
-        __syncthreads();
-    }
-    if (lane == 0) {
-        while (zero_left) zero_left = zero_next<NP, (CPLX || FFTL) ? 8 : 4, FFTL>(zr);
-        asm volatile("cp.async.bulk.wait_group 0;" ::: "memory");   // the zero rows are written
+        compute_sync();
     }
 }
 
@@ -967,7 +971,7 @@ int launch_tiles(const TileArgs &ta, int64_t n_bound, cudaStream_t s) {
     auto kern = k_tiles<NP, CPLX, FFTL>;
     NGG_CUDA(cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
     int per_sm = 0;
-    NGG_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, kern, NWT * 32, smem));
+    NGG_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, kern, (NWT + 1) * 32, smem));
     if (per_sm < 1) return fail(NGG_ERR_UNSUPPORTED, "k_tiles does not fit on an SM");
     if (n_bound > 0) {
         const int64_t zb = n_bound < (int64_t)num_sms() * 16 ? n_bound : (int64_t)num_sms() * 16;
@@ -977,7 +981,7 @@ int launch_tiles(const TileArgs &ta, int64_t n_bound, cudaStream_t s) {
         NGG_CHECK_LAUNCH("k_zero_split");
     }
     const int grid = num_sms() * per_sm;
-    kern<<<grid, NWT * 32, smem, s>>>(ta);
+    kern<<<grid, (NWT + 1) * 32, smem, s>>>(ta);
     NGG_CHECK_LAUNCH("k_tiles");
     return NGG_OK;
 }

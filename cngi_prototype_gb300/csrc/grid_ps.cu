@@ -652,11 +652,13 @@ __device__ __noinline__ bool zero_next(const ZeroRows &z) {
 //    registers (lanes 28-31 hold none). Thanks to the class order a lane
 //    reads the same record slots at every step -- one 16-byte load of its u
 //    product, one of its two v taps -- and adds them with four paired FMAs.
-//    When the track's cell changes (a warp-uniform branch) only the cells
-//    that leave the footprint are flushed to the shared tile (atomic adds)
-//    and restarted; after every chunk all cells are flushed, so that no FP32
-//    register sum runs longer than 32 steps (long sums of like-sized terms
-//    drift). The cells are absolute grid cells, so a chunk of another track
+//    The producer marks the steps where the track's cell changes (a ballot);
+//    the consumer runs through the steps between two marks with nothing but
+//    the two loads and the FMAs, and at a mark (a warp-uniform branch)
+//    flushes to the shared tile (atomic adds) only the cells that leave the
+//    footprint and restarts them; every second chunk all cells are flushed,
+//    so that no FP32 register sum runs longer than 64 steps (long sums of
+//    like-sized terms drift). The cells are absolute grid cells, so a chunk of another track
 //    simply continues accumulating into whichever cells it shares.
 // The taps come from the oversampled table staged in shared memory by a TMA
 // bulk copy. The tile is stored as (re, im) planes per pol whose column
@@ -790,7 +792,6 @@ __global__ void __launch_bounds__((NWT + 1) * 32, 1) k_tiles(const TileArgs a) {
             const int64_t n = e1 - e0;
             const int64_t rs = e0 + (n * warp) / NWT, re = e0 + (n * (warp + 1)) / NWT;
             // consumer state: the lane's cells and their accumulators
-            unsigned cur = NO_CELL;
             int ucell = -(1 << 28), vcell0 = -(1 << 28), vcell1 = -(1 << 28);
             int lu = 0, lv0 = 0, lv1 = 0;
             bool ok0 = false, ok1 = false;
@@ -832,7 +833,6 @@ __global__ void __launch_bounds__((NWT + 1) * 32, 1) k_tiles(const TileArgs a) {
                 const bool in_u = act && (unsigned)lu < (unsigned)TU;
                 ok0 = in_u && (unsigned)lv0 < (unsigned)TV;
                 ok1 = in_u && has1 && (unsigned)lv1 < (unsigned)TV;
-                cur = cuv;
             };
 
             // the chunk j's packed step of this lane (producer), loaded one
@@ -850,6 +850,7 @@ __global__ void __launch_bounds__((NWT + 1) * 32, 1) k_tiles(const TileArgs a) {
             if (rs + 1 < re) key_nx = (unsigned)(__ldg(a.keys + rs + 1) & 0xffffffffull);
             const float4 *cA = recA + kap;                                      // this lane's slots
             const float4 *cT = reinterpret_cast<const float4 *>(recT) + gr;
+            int jl = 0;
             for (int64_t j = rs; j < re; ++j) {
                 const uint2 m = m_nx;
                 const float4 d = d_nx;
@@ -858,6 +859,7 @@ __global__ void __launch_bounds__((NWT + 1) * 32, 1) k_tiles(const TileArgs a) {
                     if (j + 2 < re) key_nx = (unsigned)(__ldg(a.keys + j + 2) & 0xffffffffull);
                 }
                 // ---- producer: lane = step, records in residue-class order ----
+                unsigned chg;   // bit s: step s may change the track's cell (uniform over the warp)
                 {
                     float4 *ra = recA + lane * SUP;
                     float2 *rt = recT + lane * RT;
@@ -867,8 +869,12 @@ __global__ void __launch_bounds__((NWT + 1) * 32, 1) k_tiles(const TileArgs a) {
                         int ku = (int)((unsigned)(cu - SC) % 7u), kv = (int)((unsigned)(cv - SC) % 7u);
 #pragma unroll
                         for (int k = 0; k < SUP; ++k) {
-                            const float tu = tab[abs(os * (k - SC) + ou)];
-                            const float tv = tab[abs(os * (k - SC) + ov)];
+                            // table index |os (k - 3) + o|: o lies in [-os/2, os/2], so the sign
+                            // of the sum is the sign of k - 3
+                            const int iu = k < SC ? os * (SC - k) - ou : (k > SC ? os * (k - SC) + ou : abs(ou));
+                            const int iv = k < SC ? os * (SC - k) - ov : (k > SC ? os * (k - SC) + ov : abs(ov));
+                            const float tu = tab[iu];
+                            const float tv = tab[iv];
                             const float2 t2 = make_float2(tu, tu);
                             const float2 lo = __fmul2_rn(t2, make_float2(d.x, d.y));
                             const float2 hi = __fmul2_rn(t2, make_float2(d.z, d.w));
@@ -886,26 +892,43 @@ __global__ void __launch_bounds__((NWT + 1) * 32, 1) k_tiles(const TileArgs a) {
                     }
                     rt[SUP] = make_float2(0.f, 0.f);   // v class 7 does not exist (second row of g = 3)
                     recC[lane] = m.x;
+                    // a step whose cell differs from the previous step's (the first step of
+                    // the chunk and one after a step without a cell are marked as well;
+                    // for them the change is a no-op when the cell is the same)
+                    const unsigned prev = __shfl_up_sync(0xffffffffu, m.x, 1);
+                    chg = __ballot_sync(0xffffffffu, m.x != NO_CELL && (lane == 0 || m.x != prev));
                 }
                 __syncwarp();
-                // ---- consumer: the chunk's 32 steps ----
-#pragma unroll 8
-                for (int s = 0; s < CH; ++s) {
-                    const unsigned cuv = recC[s];
-                    if (cuv != cur && cuv != NO_CELL) change(cuv);
-                    const float4 A = cA[s * SUP];
-                    const float4 T = cT[s * (RT / 2)];   // (t0, t0, t1, t1): this lane's two v taps
-                    acc[0][0] = __ffma2_rn(make_float2(A.x, A.y), make_float2(T.x, T.y), acc[0][0]);
-                    acc[1][0] = __ffma2_rn(make_float2(A.x, A.y), make_float2(T.z, T.w), acc[1][0]);
-                    if constexpr (CPLX && NP > 1) {
-                        acc[0][1] = __ffma2_rn(make_float2(A.z, A.w), make_float2(T.x, T.y), acc[0][1]);
-                        acc[1][1] = __ffma2_rn(make_float2(A.z, A.w), make_float2(T.z, T.w), acc[1][1]);
+                // ---- consumer: the chunk's 32 steps, in runs between cell changes ----
+                const float4 *pA = cA;
+                const float4 *pT = cT;
+                int st = 0;
+                for (;;) {
+                    const int nxt = chg ? __ffs(chg) - 1 : CH;
+#pragma unroll 4
+                    for (; st < nxt; ++st, pA += SUP, pT += RT / 2) {
+                        const float4 A = *pA;
+                        const float4 T = *pT;   // (t0, t0, t1, t1): this lane's two v taps
+                        acc[0][0] = __ffma2_rn(make_float2(A.x, A.y), make_float2(T.x, T.y), acc[0][0]);
+                        acc[1][0] = __ffma2_rn(make_float2(A.x, A.y), make_float2(T.z, T.w), acc[1][0]);
+                        if constexpr (CPLX && NP > 1) {
+                            acc[0][1] = __ffma2_rn(make_float2(A.z, A.w), make_float2(T.x, T.y), acc[0][1]);
+                            acc[1][1] = __ffma2_rn(make_float2(A.z, A.w), make_float2(T.z, T.w), acc[1][1]);
+                        }
                     }
+                    if (nxt >= CH) break;
+                    change(recC[nxt]);
+                    chg &= chg - 1u;
                 }
-                // bound the register sums to one chunk (32 steps)
-                flush(0); zero(0); flush(1); zero(1);
+                // bound the register sums to two chunks (64 steps)
+                if (++jl == 2) {
+                    jl = 0;
+                    flush(0); zero(0); flush(1); zero(1);
+                }
                 __syncwarp();   // the producer of the next chunk overwrites the records
             }
+            flush(0);
+            flush(1);
             compute_sync();   // every warp's cells are in the tile
         }
 

@@ -643,7 +643,7 @@ __device__ __noinline__ bool zero_next(const ZeroRows &z) {
 //  * producer: lane s takes step s of the chunk (its packed record, loaded
 //    from global memory one chunk ahead) and writes to the warp's shared
 //    record, in residue-class order, the 7 products tap_u(k) * weighted data
-//    (both pols) and the 7 v taps (each duplicated into a pair), plus the
+//    (both pols) and the 7 v taps, plus the
 //    step's cell: the product for u tap k goes to class (cu - 3 + k) mod 7,
 //    the class whose cell that tap reaches;
 //  * consumer: the 49 footprint cells are owned in Romein's residue classes:
@@ -651,7 +651,8 @@ __device__ __noinline__ bool zero_next(const ZeroRows &z) {
 //    (0..3), holds the cells of u class kappa and v classes 2g and 2g+1 in
 //    registers (lanes 28-31 hold none). Thanks to the class order a lane
 //    reads the same record slots at every step -- one 16-byte load of its u
-//    product, one of its two v taps -- and adds them with four paired FMAs.
+//    product, one 8-byte load of its two v taps -- and adds them with four
+//    paired FMAs.
 //    The producer marks the steps where the track's cell changes (a ballot);
 //    the consumer runs through the steps between two marks with nothing but
 //    the two loads and the FMAs, and at a mark (a warp-uniform branch)
@@ -665,8 +666,8 @@ __device__ __noinline__ bool zero_next(const ZeroRows &z) {
 // index is XOR-swizzled by the row, so the flush atomics of the 7 u classes
 // of one v cell fall into different banks.
 constexpr int NWT = 24;                  // warps per CTA (one CTA per SM)
-constexpr int RT = 10;                   // float2 per step of v-tap pairs (16-byte rows; 8 used)
-constexpr int WARP_REC_BYTES = CH * SUP * 16 + CH * RT * 8 + CH * 4;
+constexpr int RT = 10;                   // floats per step of v taps (8 used; the odd-pair stride spreads banks)
+constexpr int WARP_REC_BYTES = CH * SUP * 16 + CH * RT * 4 + CH * 4;
 
 // the tile kernel's compute warps (all but the zero-fill warp)
 __device__ __forceinline__ void compute_sync() { asm volatile("bar.sync 1, %0;" ::"n"(NWT * 32) : "memory"); }
@@ -731,7 +732,7 @@ __global__ void __launch_bounds__((NWT + 1) * 32, 1) k_tiles(const TileArgs a) {
     const unsigned zs = (unsigned)__cvta_generic_to_shared(zbuf);
 
     float4 *recA = reinterpret_cast<float4 *>(recs + (size_t)warp * WARP_REC_BYTES);   // [CH][SUP] by u class
-    float2 *recT = reinterpret_cast<float2 *>(recA + CH * SUP);                         // [CH][RT] by v class
+    float *recT = reinterpret_cast<float *>(recA + CH * SUP);                           // [CH][RT] by v class
     unsigned *recC = reinterpret_cast<unsigned *>(recT + CH * RT);                      // [CH]
 
     const int64_t NT = (int64_t)a.ntu * a.ntv;
@@ -849,7 +850,7 @@ __global__ void __launch_bounds__((NWT + 1) * 32, 1) k_tiles(const TileArgs a) {
             if (rs < re) fetch((unsigned)(__ldg(a.keys + rs) & 0xffffffffull));
             if (rs + 1 < re) key_nx = (unsigned)(__ldg(a.keys + rs + 1) & 0xffffffffull);
             const float4 *cA = recA + kap;                                      // this lane's slots
-            const float4 *cT = reinterpret_cast<const float4 *>(recT) + gr;
+            const float2 *cT = reinterpret_cast<const float2 *>(recT) + gr;
             int jl = 0;
             for (int64_t j = rs; j < re; ++j) {
                 const uint2 m = m_nx;
@@ -862,7 +863,7 @@ __global__ void __launch_bounds__((NWT + 1) * 32, 1) k_tiles(const TileArgs a) {
                 unsigned chg;   // bit s: step s may change the track's cell (uniform over the warp)
                 {
                     float4 *ra = recA + lane * SUP;
-                    float2 *rt = recT + lane * RT;
+                    float *rt = recT + lane * RT;
                     if (m.x != NO_CELL) {
                         const int cu = (int)(m.x >> 16), cv = (int)(m.x & 0xffffu);
                         const int ou = (int)(m.y & 0xffffu) - 32768, ov = (int)(m.y >> 16) - 32768;
@@ -879,7 +880,7 @@ __global__ void __launch_bounds__((NWT + 1) * 32, 1) k_tiles(const TileArgs a) {
                             const float2 lo = __fmul2_rn(t2, make_float2(d.x, d.y));
                             const float2 hi = __fmul2_rn(t2, make_float2(d.z, d.w));
                             ra[ku] = make_float4(lo.x, lo.y, hi.x, hi.y);
-                            rt[kv] = make_float2(tv, tv);
+                            rt[kv] = tv;
                             ku = ku == 6 ? 0 : ku + 1;
                             kv = kv == 6 ? 0 : kv + 1;
                         }
@@ -887,10 +888,10 @@ __global__ void __launch_bounds__((NWT + 1) * 32, 1) k_tiles(const TileArgs a) {
 #pragma unroll
                         for (int k = 0; k < SUP; ++k) {
                             ra[k] = make_float4(0.f, 0.f, 0.f, 0.f);
-                            rt[k] = make_float2(0.f, 0.f);
+                            rt[k] = 0.f;
                         }
                     }
-                    rt[SUP] = make_float2(0.f, 0.f);   // v class 7 does not exist (second row of g = 3)
+                    rt[SUP] = 0.f;   // v class 7 does not exist (second row of g = 3)
                     recC[lane] = m.x;
                     // a step whose cell differs from the previous step's (the first step of
                     // the chunk and one after a step without a cell are marked as well;
@@ -901,19 +902,20 @@ __global__ void __launch_bounds__((NWT + 1) * 32, 1) k_tiles(const TileArgs a) {
                 __syncwarp();
                 // ---- consumer: the chunk's 32 steps, in runs between cell changes ----
                 const float4 *pA = cA;
-                const float4 *pT = cT;
+                const float2 *pT = cT;
                 int st = 0;
                 for (;;) {
                     const int nxt = chg ? __ffs(chg) - 1 : CH;
 #pragma unroll 4
                     for (; st < nxt; ++st, pA += SUP, pT += RT / 2) {
                         const float4 A = *pA;
-                        const float4 T = *pT;   // (t0, t0, t1, t1): this lane's two v taps
-                        acc[0][0] = __ffma2_rn(make_float2(A.x, A.y), make_float2(T.x, T.y), acc[0][0]);
-                        acc[1][0] = __ffma2_rn(make_float2(A.x, A.y), make_float2(T.z, T.w), acc[1][0]);
+                        const float2 t = *pT;   // this lane's two v taps
+                        const float2 T0 = make_float2(t.x, t.x), T1 = make_float2(t.y, t.y);
+                        acc[0][0] = __ffma2_rn(make_float2(A.x, A.y), T0, acc[0][0]);
+                        acc[1][0] = __ffma2_rn(make_float2(A.x, A.y), T1, acc[1][0]);
                         if constexpr (CPLX && NP > 1) {
-                            acc[0][1] = __ffma2_rn(make_float2(A.z, A.w), make_float2(T.x, T.y), acc[0][1]);
-                            acc[1][1] = __ffma2_rn(make_float2(A.z, A.w), make_float2(T.z, T.w), acc[1][1]);
+                            acc[0][1] = __ffma2_rn(make_float2(A.z, A.w), T0, acc[0][1]);
+                            acc[1][1] = __ffma2_rn(make_float2(A.z, A.w), T1, acc[1][1]);
                         }
                     }
                     if (nxt >= CH) break;

@@ -665,10 +665,7 @@ __device__ __noinline__ bool zero_next(const ZeroRows &z) {
 // bulk copy. The tile is stored as (re, im) planes per pol whose column
 // index is XOR-swizzled by the row, so the flush atomics of the 7 u classes
 // of one v cell fall into different banks.
-// compute warps per CTA (one CTA per SM) plus the zero-fill warp: 16 warps,
-// four per scheduler partition, whose quarter of the register file then
-// holds up to 128 registers a thread
-constexpr int NWT = 15;
+constexpr int NWT = 16;                  // compute warps per CTA (one CTA per SM, plus the zero-fill warp)
 constexpr int NTRK = 4;                  // tracks a warp grids at once (one per group of 8 lanes)
 constexpr int RSTEP = 8;                 // steps of each track per producer round
 constexpr int NREC = NTRK * RSTEP;       // step records per round (one per lane)
@@ -689,7 +686,7 @@ __device__ __forceinline__ int residue_cell(int lo, int cls) {
 }
 
 template <int NP, bool CPLX, bool FFTL>
-__global__ void __launch_bounds__((NWT + 1) * 32, 1) k_tiles(const TileArgs a) {
+__global__ void __maxnreg__(120) k_tiles(const TileArgs a) {
     extern __shared__ __align__(16) unsigned char smem[];
     constexpr int NPL = CPLX ? 2 * NP : NP;   // float planes of the tile
     constexpr int NA = CPLX ? NP : 1;         // float2 accumulators per cell

@@ -665,11 +665,9 @@ __device__ __noinline__ bool zero_next(const ZeroRows &z) {
 // bulk copy. The tile is stored as (re, im) planes per pol whose column
 // index is XOR-swizzled by the row, so the flush atomics of the 7 u classes
 // of one v cell fall into different banks.
-constexpr int NWT = 16;                  // compute warps per CTA (one CTA per SM, plus the zero-fill warp)
-constexpr int NTRK = 4;                  // tracks a warp grids at once (one per group of 8 lanes)
-constexpr int RSTEP = 8;                 // steps of each track per producer round
-constexpr int NREC = NTRK * RSTEP;       // step records per round (one per lane)
-constexpr int WARP_REC_BYTES = NREC * SUP * 16 + NREC * 8 * 4 + NREC * 4;
+constexpr int NWT = 24;                  // warps per CTA (one CTA per SM)
+constexpr int RT = 10;                   // floats per step of v taps (8 used; the odd-pair stride spreads banks)
+constexpr int WARP_REC_BYTES = CH * SUP * 16 + CH * RT * 4 + CH * 4;
 
 // the tile kernel's compute warps (all but the zero-fill warp)
 __device__ __forceinline__ void compute_sync() { asm volatile("bar.sync 1, %0;" ::"n"(NWT * 32) : "memory"); }
@@ -686,7 +684,7 @@ __device__ __forceinline__ int residue_cell(int lo, int cls) {
 }
 
 template <int NP, bool CPLX, bool FFTL>
-__global__ void __maxnreg__(120) k_tiles(const TileArgs a) {
+__global__ void __launch_bounds__((NWT + 1) * 32, 1) k_tiles(const TileArgs a) {
     extern __shared__ __align__(16) unsigned char smem[];
     constexpr int NPL = CPLX ? 2 * NP : NP;   // float planes of the tile
     constexpr int NA = CPLX ? NP : 1;         // float2 accumulators per cell
@@ -733,9 +731,9 @@ __global__ void __maxnreg__(120) k_tiles(const TileArgs a) {
     __syncthreads();
     const unsigned zs = (unsigned)__cvta_generic_to_shared(zbuf);
 
-    float4 *recA = reinterpret_cast<float4 *>(recs + (size_t)warp * WARP_REC_BYTES);   // [NREC][SUP] by u class
-    float *recT = reinterpret_cast<float *>(recA + NREC * SUP);                         // [NREC][8] by v class
-    unsigned *recC = reinterpret_cast<unsigned *>(recT + NREC * 8);                     // [NREC]
+    float4 *recA = reinterpret_cast<float4 *>(recs + (size_t)warp * WARP_REC_BYTES);   // [CH][SUP] by u class
+    float *recT = reinterpret_cast<float *>(recA + CH * SUP);                           // [CH][RT] by v class
+    unsigned *recC = reinterpret_cast<unsigned *>(recT + CH * RT);                      // [CH]
 
     const int64_t NT = (int64_t)a.ntu * a.ntv;
     const int cu_c = (int)(a.nu / 2), cv_c = (int)(a.nv / 2);
@@ -749,11 +747,12 @@ __global__ void __maxnreg__(120) k_tiles(const TileArgs a) {
     const int64_t n_zero_items = (int64_t)a.n_img * NP * nrb;
     const int os = a.os;
 
-    // this lane's track group and u residue class (consumer); lane 7 of a
-    // group holds no cells
-    const int grp = lane >> 3, kap = lane & 7;
-    const bool act = kap < 7;
-    const int kapr = act ? kap : 0;   // the idle lane reads a valid slot
+    // this lane's residue classes (consumer)
+    const bool act = lane < 28;
+    const int kap = lane % 7, g = lane / 7;
+    const int rho0 = 2 * g, rho1 = 2 * g + 1;
+    const bool has1 = act && g < 3;
+    const int gr = g < 3 ? g : 3;   // lanes 28-31 read a valid slot (and never flush)
 
     // Warp NWT zeroes the rows outside the busy box: each of its lanes takes
     // blocks of rows from a counter and zeroes them with TMA bulk stores from
@@ -793,28 +792,20 @@ __global__ void __maxnreg__(120) k_tiles(const TileArgs a) {
             // ---------------- busy tile: this warp's chunk range ----------------
             const int64_t n = e1 - e0;
             const int64_t rs = e0 + (n * warp) / NWT, re = e0 + (n * (warp + 1)) / NWT;
-            // the warp's range in NTRK contiguous parts, one per track group
-            const int64_t gs = rs + ((re - rs) * grp) / NTRK, ge = rs + ((re - rs) * (grp + 1)) / NTRK;
-            const int glen = (int)(ge - gs);
-            int maxlen = glen;
-            maxlen = max(maxlen, __shfl_xor_sync(0xffffffffu, maxlen, 8));
-            maxlen = max(maxlen, __shfl_xor_sync(0xffffffffu, maxlen, 16));
-            // consumer state: the lane's column cell, its 7 row cells (by v
-            // class) and their accumulators; bit r of okv: cell r is in the tile
-            int ucell = -(1 << 28);
-            int vcell[SUP];
-            unsigned okv = 0;
-            float2 acc[SUP][NA];
+            // consumer state: the lane's cells and their accumulators
+            int ucell = -(1 << 28), vcell0 = -(1 << 28), vcell1 = -(1 << 28);
+            int lu = 0, lv0 = 0, lv1 = 0;
+            bool ok0 = false, ok1 = false;
+            float2 acc[2][NA];
 #pragma unroll
-            for (int r = 0; r < SUP; ++r) {
-                vcell[r] = -(1 << 28);
+            for (int r = 0; r < 2; ++r)
 #pragma unroll
                 for (int q = 0; q < NA; ++q) acc[r][q] = make_float2(0.f, 0.f);
-            }
 
             auto flush = [&](int r) {
-                if (!((okv >> r) & 1u)) return;
-                const int ad = tile_addr(ucell - u0, vcell[r] - v0);
+                const bool ok = r ? ok1 : ok0;
+                if (!ok) return;
+                const int ad = tile_addr(lu, r ? lv1 : lv0);
 #pragma unroll
                 for (int q = 0; q < NA; ++q) {
                     const float2 x = acc[r][q];
@@ -831,69 +822,48 @@ __global__ void __maxnreg__(120) k_tiles(const TileArgs a) {
 #pragma unroll
                 for (int q = 0; q < NA; ++q) acc[r][q] = make_float2(0.f, 0.f);
             };
-            // the track moves to footprint cell cuv: cells that leave the
-            // footprint are flushed and restarted
             auto change = [&](unsigned cuv) {
                 const int lo_u = (int)(cuv >> 16) - SC, lo_v = (int)(cuv & 0xffffu) - SC;
                 const int nu_ = residue_cell(lo_u, kap);
+                const int nv0 = residue_cell(lo_v, rho0), nv1 = residue_cell(lo_v, rho1);
                 const bool cc = nu_ != ucell;
-                const bool in_u = act && (unsigned)(nu_ - u0) < (unsigned)TU;
-                const int mv = (int)((unsigned)lo_v % 7u);
-#pragma unroll
-                for (int r = 0; r < SUP; ++r) {
-                    int dd = r - mv;
-                    if (dd < 0) dd += 7;
-                    const int nv = lo_v + dd;
-                    if (cc || nv != vcell[r]) {
-                        flush(r);
-                        zero(r);
-                        vcell[r] = nv;
-                    }
-                    okv = (okv & ~(1u << r)) | ((in_u && (unsigned)(nv - v0) < (unsigned)TV) ? (1u << r) : 0u);
-                }
-                ucell = nu_;
+                if (cc || nv0 != vcell0) { flush(0); zero(0); }
+                if (cc || nv1 != vcell1) { flush(1); zero(1); }
+                ucell = nu_; vcell0 = nv0; vcell1 = nv1;
+                lu = ucell - u0; lv0 = vcell0 - v0; lv1 = vcell1 - v0;
+                const bool in_u = act && (unsigned)lu < (unsigned)TU;
+                ok0 = in_u && (unsigned)lv0 < (unsigned)TV;
+                ok1 = in_u && has1 && (unsigned)lv1 < (unsigned)TV;
             };
 
-            // this lane's packed step of the next round (producer), loaded a
-            // round ahead; the group's chunk keys a chunk ahead
+            // the chunk j's packed step of this lane (producer), loaded one
+            // chunk ahead; the chunk keys two chunks ahead, so that a data
+            // load never waits for the key load it depends on
             uint2 m_nx = make_uint2(NO_CELL, 0u);
             float4 d_nx = make_float4(0.f, 0.f, 0.f, 0.f);
-            auto key_of = [&](int jj) -> unsigned {
-                return jj < glen ? (unsigned)(__ldg(a.keys + gs + jj) & 0xffffffffull) : NO_CELL;
-            };
-            auto fetch = [&](unsigned chu, int r) {
-                if (chu == NO_CELL) {
-                    m_nx = make_uint2(NO_CELL, 0u);
-                    return;
-                }
-                const int64_t ri = (int64_t)chu * CH + r * RSTEP + kap;
+            unsigned key_nx = 0;
+            auto fetch = [&](unsigned chu) {
+                const int64_t ri = (int64_t)chu * CH + lane;
                 m_nx = __ldg(a.meta + ri);
                 d_nx = __ldg(a.wvp + ri);
             };
-            unsigned key_cur = key_of(0), key_nx = key_of(1);
-            fetch(key_cur, 0);
-            unsigned last = NO_CELL;   // cell of the group's previous step
-            const float4 *cA = recA + grp * RSTEP * SUP + kapr;                  // this lane's slots
-            const float4 *cT = reinterpret_cast<const float4 *>(recT) + grp * RSTEP * 2;
-            const unsigned *cC = recC + grp * RSTEP;
+            if (rs < re) fetch((unsigned)(__ldg(a.keys + rs) & 0xffffffffull));
+            if (rs + 1 < re) key_nx = (unsigned)(__ldg(a.keys + rs + 1) & 0xffffffffull);
+            const float4 *cA = recA + kap;                                      // this lane's slots
+            const float2 *cT = reinterpret_cast<const float2 *>(recT) + gr;
             int jl = 0;
-            const int rounds = maxlen * (CH / RSTEP);
-            for (int t = 0; t < rounds; ++t) {
-                const int r = t % (CH / RSTEP);
+            for (int64_t j = rs; j < re; ++j) {
                 const uint2 m = m_nx;
                 const float4 d = d_nx;
-                if (t + 1 < rounds) {
-                    if (r == CH / RSTEP - 1) {
-                        key_cur = key_nx;
-                        key_nx = key_of(t / (CH / RSTEP) + 2);
-                    }
-                    fetch(key_cur, (t + 1) % (CH / RSTEP));
+                if (j + 1 < re) {
+                    fetch(key_nx);
+                    if (j + 2 < re) key_nx = (unsigned)(__ldg(a.keys + j + 2) & 0xffffffffull);
                 }
-                // ---- producer: lane = one step record, in residue-class order ----
-                unsigned chg;   // bit 8g + s: step s of group g may change its track's cell
+                // ---- producer: lane = step, records in residue-class order ----
+                unsigned chg;   // bit s: step s may change the track's cell (uniform over the warp)
                 {
                     float4 *ra = recA + lane * SUP;
-                    float *rt = recT + lane * 8;
+                    float *rt = recT + lane * RT;
                     if (m.x != NO_CELL) {
                         const int cu = (int)(m.x >> 16), cv = (int)(m.x & 0xffffu);
                         const int ou = (int)(m.y & 0xffffu) - 32768, ov = (int)(m.y >> 16) - 32768;
@@ -921,43 +891,46 @@ __global__ void __maxnreg__(120) k_tiles(const TileArgs a) {
                             rt[k] = 0.f;
                         }
                     }
-                    rt[SUP] = 0.f;
+                    rt[SUP] = 0.f;   // v class 7 does not exist (second row of g = 3)
                     recC[lane] = m.x;
-                    // a step whose cell differs from its track's previous step (after a
-                    // step without a cell the mark may be spurious: the change is then a
-                    // no-op)
-                    const unsigned up = __shfl_up_sync(0xffffffffu, m.x, 1);
-                    const unsigned prev = kap == 0 ? last : up;
-                    chg = __ballot_sync(0xffffffffu, m.x != NO_CELL && m.x != prev);
-                    last = __shfl_sync(0xffffffffu, m.x, grp * RSTEP + RSTEP - 1);
+                    // a step whose cell differs from the previous step's (the first step of
+                    // the chunk and one after a step without a cell are marked as well;
+                    // for them the change is a no-op when the cell is the same)
+                    const unsigned prev = __shfl_up_sync(0xffffffffu, m.x, 1);
+                    chg = __ballot_sync(0xffffffffu, m.x != NO_CELL && (lane == 0 || m.x != prev));
                 }
                 __syncwarp();
-                // ---- consumer: the round's steps, the four tracks side by side ----
-#pragma unroll 2
-                for (int st = 0; st < RSTEP; ++st) {
-                    if (chg & (0x01010101u << st)) {   // some track changes cell at this step
-                        if (chg & (1u << (grp * RSTEP + st))) change(cC[st]);
+                // ---- consumer: the chunk's 32 steps, in runs between cell changes ----
+                const float4 *pA = cA;
+                const float2 *pT = cT;
+                int st = 0;
+                for (;;) {
+                    const int nxt = chg ? __ffs(chg) - 1 : CH;
+#pragma unroll 4
+                    for (; st < nxt; ++st, pA += SUP, pT += RT / 2) {
+                        const float4 A = *pA;
+                        const float2 t = *pT;   // this lane's two v taps
+                        const float2 T0 = make_float2(t.x, t.x), T1 = make_float2(t.y, t.y);
+                        acc[0][0] = __ffma2_rn(make_float2(A.x, A.y), T0, acc[0][0]);
+                        acc[1][0] = __ffma2_rn(make_float2(A.x, A.y), T1, acc[1][0]);
+                        if constexpr (CPLX && NP > 1) {
+                            acc[0][1] = __ffma2_rn(make_float2(A.z, A.w), T0, acc[0][1]);
+                            acc[1][1] = __ffma2_rn(make_float2(A.z, A.w), T1, acc[1][1]);
+                        }
                     }
-                    const float4 A = cA[st * SUP];
-                    const float4 T03 = cT[2 * st], T47 = cT[2 * st + 1];   // the step's 7 v taps by class
-                    const float tv[SUP] = {T03.x, T03.y, T03.z, T03.w, T47.x, T47.y, T47.z};
-#pragma unroll
-                    for (int rr = 0; rr < SUP; ++rr) {
-                        const float2 T2 = make_float2(tv[rr], tv[rr]);
-                        acc[rr][0] = __ffma2_rn(make_float2(A.x, A.y), T2, acc[rr][0]);
-                        if constexpr (CPLX && NP > 1) acc[rr][1] = __ffma2_rn(make_float2(A.z, A.w), T2, acc[rr][1]);
-                    }
+                    if (nxt >= CH) break;
+                    change(recC[nxt]);
+                    chg &= chg - 1u;
                 }
                 // bound the register sums to two chunks (64 steps)
-                if (r == CH / RSTEP - 1 && ++jl == 2) {
+                if (++jl == 2) {
                     jl = 0;
-#pragma unroll
-                    for (int rr = 0; rr < SUP; ++rr) { flush(rr); zero(rr); }
+                    flush(0); zero(0); flush(1); zero(1);
                 }
-                __syncwarp();   // the producer of the next round overwrites the records
+                __syncwarp();   // the producer of the next chunk overwrites the records
             }
-#pragma unroll
-            for (int rr = 0; rr < SUP; ++rr) flush(rr);
+            flush(0);
+            flush(1);
             compute_sync();   // every warp's cells are in the tile
         }
 

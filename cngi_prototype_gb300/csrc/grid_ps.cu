@@ -140,7 +140,25 @@ struct PackArgs {
     const unsigned char *flag;   // (T,B,c_stride,P), nonzero = flagged visibility (DATA mode), or NULL
     int64_t dnu, dnv, n_img;
     int continuum;
+    // cell_half's constants: K = (2 C + 1) os per axis, 1 / os, its margin;
+    // half_ok = 0 where K >= 2^24 (then cell_pair serves every step)
+    float ku, kv, inv_os, margin0;
+    int half_ok;
 };
+
+// cell_pair, then the FP64 chain: the packing pass's rare path (a step near a
+// rounding boundary), kept out of line so that its registers do not weigh on
+// the common path. axis 0 = u, 1 = v; xyz points at the step's uvw row.
+static __device__ __noinline__ void cell_slow(float xh, float xl, const ChanParms *cpp, int axis, const double *xyz,
+                                              int center, int os, int &idx, int &off) {
+    const ChanParms cp = *cpp;
+    const float sh = axis ? cp.svh : cp.suh, sl = axis ? cp.svl : cp.sul;
+    if (cell_pair(xh, xl, sh, sl, false, center, os, idx, off)) return;
+    long long i64, o64;
+    cell_fp64(xyz[axis], axis ? cp.sv : cp.su, false, center, os, i64, o64);
+    idx = (int)max(min(i64, (long long)1 << 30), -((long long)1 << 30));
+    off = (int)o64;
+}
 
 // The reference's nearest-cell weight lookup (_standard_imaging_weight_degrid_jit,
 // _standard_grid.py:466-518), for one (time, baseline, channel): the step's
@@ -209,6 +227,10 @@ __global__ void __launch_bounds__(256, 4) k_pack(const PackArgs a) {
     const bool c_ok = c < a.C;
     ChanParms cp{};
     if (c_ok) cp = a.chan[c];
+    // cell_half's scales for this channel (2 os s as pairs)
+    float s2uh, s2ul, s2vh, s2vl;
+    scale_pair(cp.suh, cp.sul, (float)(2 * a.os), s2uh, s2ul);
+    scale_pair(cp.svh, cp.svl, (float)(2 * a.os), s2vh, s2vl);
     float4 us4[4];
     float wl[4][NP];
     float2 vl[4][NP];
@@ -240,18 +262,10 @@ __global__ void __launch_bounds__(256, 4) k_pack(const PackArgs a) {
         const float4 us = us4[i];
         if (c_ok && t < a.T && !isnan(us.x) && !isnan(us.z)) {
             int cu, ou, cv, ov;
-            if (!cell_pair(us.x, us.y, cp.suh, cp.sul, false, cu_c, a.os, cu, ou)) {
-                long long i64, o64;
-                cell_fp64(a.uvw[(t * a.B + b) * 3 + 0], cp.su, false, cu_c, a.os, i64, o64);
-                cu = (int)max(min(i64, (long long)1 << 30), -((long long)1 << 30));
-                ou = (int)o64;
-            }
-            if (!cell_pair(us.z, us.w, cp.svh, cp.svl, false, cv_c, a.os, cv, ov)) {
-                long long i64, o64;
-                cell_fp64(a.uvw[(t * a.B + b) * 3 + 1], cp.sv, false, cv_c, a.os, i64, o64);
-                cv = (int)max(min(i64, (long long)1 << 30), -((long long)1 << 30));
-                ov = (int)o64;
-            }
+            if (!(a.half_ok && cell_half(us.x, us.y, s2uh, s2ul, a.ku, a.os, a.inv_os, a.margin0, cu, ou)))
+                cell_slow(us.x, us.y, a.chan + c, 0, a.uvw + (t * a.B + b) * 3, cu_c, a.os, cu, ou);
+            if (!(a.half_ok && cell_half(us.z, us.w, s2vh, s2vl, a.kv, a.os, a.inv_os, a.margin0, cv, ov)))
+                cell_slow(us.z, us.w, a.chan + c, 1, a.uvw + (t * a.B + b) * 3, cv_c, a.os, cv, ov);
             if (cu - SC >= 0 && cu + SC < a.nu && cv - SC >= 0 && cv + SC < a.nv) {
                 const int64_t base = ((t * a.B + b) * a.c_stride + a.c_off + c) * a.P + a.p0;
                 float w[NP];
@@ -642,10 +656,9 @@ __device__ __noinline__ bool zero_next(const ZeroRows &z) {
 // handles one 32-step chunk at a time in two phases:
 //  * producer: lane s takes step s of the chunk (its packed record, loaded
 //    from global memory one chunk ahead) and writes to the warp's shared
-//    record, in residue-class order, the 7 products tap_u(k) * weighted data
-//    (both pols) and the 7 v taps, plus the
-//    step's cell: the product for u tap k goes to class (cu - 3 + k) mod 7,
-//    the class whose cell that tap reaches;
+//    record, in residue-class order, the 7 products tap_u * weighted data
+//    (both pols) and the 7 v taps, plus the step's cell: class c holds the
+//    tap whose cell has class c, tap k = (c - (cu - 3)) mod 7;
 //  * consumer: the 49 footprint cells are owned in Romein's residue classes:
 //    lane (kappa, g), kappa = lane % 7 the u class (u mod 7), g = lane / 7
 //    (0..3), holds the cells of u class kappa and v classes 2g and 2g+1 in
@@ -666,7 +679,8 @@ __device__ __noinline__ bool zero_next(const ZeroRows &z) {
 // index is XOR-swizzled by the row, so the flush atomics of the 7 u classes
 // of one v cell fall into different banks.
 constexpr int NWT = 24;                  // warps per CTA (one CTA per SM)
-constexpr int RT = 10;                   // floats per step of v taps (8 used; the odd-pair stride spreads banks)
+constexpr int RT = 12;                   // floats per step of v taps (8 used; a 48-byte row keeps the
+                                         // 16-byte stores of a quarter-warp in different banks)
 constexpr int WARP_REC_BYTES = CH * SUP * 16 + CH * RT * 4 + CH * 4;
 
 // the tile kernel's compute warps (all but the zero-fill warp)
@@ -863,40 +877,49 @@ __global__ void __launch_bounds__((NWT + 1) * 32, 1) k_tiles(const TileArgs a) {
                 unsigned chg;   // bit s: step s may change the track's cell (uniform over the warp)
                 {
                     float4 *ra = recA + lane * SUP;
-                    float *rt = recT + lane * RT;
+                    float4 *rt = reinterpret_cast<float4 *>(recT + lane * RT);
                     if (m.x != NO_CELL) {
                         const int cu = (int)(m.x >> 16), cv = (int)(m.x & 0xffffu);
                         const int ou = (int)(m.y & 0xffffu) - 32768, ov = (int)(m.y >> 16) - 32768;
-                        int ku = (int)((unsigned)(cu - SC) % 7u), kv = (int)((unsigned)(cv - SC) % 7u);
+                        // the class of tap 0's cell
+                        const int ku = (int)((unsigned)(cu - SC) % 7u), kv = (int)((unsigned)(cv - SC) % 7u);
+                        float tv[SUP + 1];
 #pragma unroll
-                        for (int k = 0; k < SUP; ++k) {
-                            // table index |os (k - 3) + o|: o lies in [-os/2, os/2], so the sign
-                            // of the sum is the sign of k - 3
-                            const int iu = k < SC ? os * (SC - k) - ou : (k > SC ? os * (k - SC) + ou : abs(ou));
-                            const int iv = k < SC ? os * (SC - k) - ov : (k > SC ? os * (k - SC) + ov : abs(ov));
-                            const float tu = tab[iu];
-                            const float tv = tab[iv];
+                        for (int c = 0; c < SUP; ++c) {
+                            // class c holds tap k = (c - k0) mod 7, whose table index is
+                            // |os (k - 3) + o| (o lies in [-os/2, os/2]); the classes are
+                            // written in order, so a quarter-warp's 16-byte stores fall into
+                            // different banks
+                            const int kku = c - ku + (c < ku ? SUP : 0);
+                            const int kkv = c - kv + (c < kv ? SUP : 0);
+                            const float tu = tab[abs(os * (kku - SC) + ou)];
+                            tv[c] = tab[abs(os * (kkv - SC) + ov)];
                             const float2 t2 = make_float2(tu, tu);
                             const float2 lo = __fmul2_rn(t2, make_float2(d.x, d.y));
                             const float2 hi = __fmul2_rn(t2, make_float2(d.z, d.w));
-                            ra[ku] = make_float4(lo.x, lo.y, hi.x, hi.y);
-                            rt[kv] = tv;
-                            ku = ku == 6 ? 0 : ku + 1;
-                            kv = kv == 6 ? 0 : kv + 1;
+                            ra[c] = make_float4(lo.x, lo.y, hi.x, hi.y);
                         }
+                        tv[SUP] = 0.f;   // v class 7 does not exist (second row of g = 3)
+                        rt[0] = make_float4(tv[0], tv[1], tv[2], tv[3]);
+                        rt[1] = make_float4(tv[4], tv[5], tv[6], tv[7]);
                     } else {
 #pragma unroll
-                        for (int k = 0; k < SUP; ++k) {
-                            ra[k] = make_float4(0.f, 0.f, 0.f, 0.f);
-                            rt[k] = 0.f;
-                        }
+                        for (int c = 0; c < SUP; ++c) ra[c] = make_float4(0.f, 0.f, 0.f, 0.f);
+                        rt[0] = make_float4(0.f, 0.f, 0.f, 0.f);
+                        rt[1] = make_float4(0.f, 0.f, 0.f, 0.f);
                     }
-                    rt[SUP] = 0.f;   // v class 7 does not exist (second row of g = 3)
                     recC[lane] = m.x;
-                    // a step whose cell differs from the previous step's (the first step of
-                    // the chunk and one after a step without a cell are marked as well;
-                    // for them the change is a no-op when the cell is the same)
-                    const unsigned prev = __shfl_up_sync(0xffffffffu, m.x, 1);
+                    // a step whose cell differs from the cell of the chunk's last step
+                    // before it that has one (steps without a cell add zeros to whatever
+                    // cells are current, so they do not end a run; the chunk's first step
+                    // with a cell is marked as well, a no-op when its cell is current)
+                    unsigned last = m.x;   // the cell of this step or of the latest step before it that has one
+#pragma unroll
+                    for (int o = 1; o < 32; o <<= 1) {
+                        const unsigned t = __shfl_up_sync(0xffffffffu, last, o);
+                        if (lane >= o && last == NO_CELL) last = t;
+                    }
+                    const unsigned prev = __shfl_up_sync(0xffffffffu, last, 1);
                     chg = __ballot_sync(0xffffffffu, m.x != NO_CELL && (lane == 0 || m.x != prev));
                 }
                 __syncwarp();
@@ -1029,14 +1052,25 @@ __global__ void k_cell_indices(int64_t n_rows, int64_t C, const double *uvw, con
     const Split x = split_double(u), y = split_double(v);
     int cu = 0, cv = 0, ou = 0, ov = 0;
     unsigned long long fb = 0;
-    if (!cell_pair(x.hi, x.lo, a.hi, a.lo, mirror != 0, (int)(nu / 2), os, cu, ou)) {
+    // the packing pass's chain: cell_half, then cell_pair, then FP64
+    const int cu_c = (int)(nu / 2), cv_c = (int)(nv / 2);
+    const float os2 = (float)(2 * os) * (mirror ? -1.f : 1.f);
+    float s2uh, s2ul, s2vh, s2vl;
+    scale_pair(a.hi, a.lo, os2, s2uh, s2ul);
+    scale_pair(b.hi, b.lo, os2, s2vh, s2vl);
+    const bool half_ok = os >= 1 && (int64_t)(2 * cu_c + 1) * os < (1 << 24) && (int64_t)(2 * cv_c + 1) * os < (1 << 24);
+    const float Ku = (float)((2 * cu_c + 1) * os), Kv = (float)((2 * cv_c + 1) * os);
+    const float inv_os = 1.0f / (float)max(os, 1), margin0 = fmaf(2e-8f, (float)os, 2e-7f);
+    if (!(half_ok && cell_half(x.hi, x.lo, s2uh, s2ul, Ku, os, inv_os, margin0, cu, ou)) &&
+        !cell_pair(x.hi, x.lo, a.hi, a.lo, mirror != 0, cu_c, os, cu, ou)) {
         long long i64, o64;
         cell_fp64(u, su, mirror != 0, (int)(nu / 2), os, i64, o64);
         cu = (int)max(min(i64, (long long)1 << 30), -((long long)1 << 30));
         ou = (int)max(min(o64, (long long)1 << 30), -((long long)1 << 30));
         ++fb;
     }
-    if (!cell_pair(y.hi, y.lo, b.hi, b.lo, mirror != 0, (int)(nv / 2), os, cv, ov)) {
+    if (!(half_ok && cell_half(y.hi, y.lo, s2vh, s2vl, Kv, os, inv_os, margin0, cv, ov)) &&
+        !cell_pair(y.hi, y.lo, b.hi, b.lo, mirror != 0, cv_c, os, cv, ov)) {
         long long i64, o64;
         cell_fp64(v, sv, mirror != 0, (int)(nv / 2), os, i64, o64);
         cv = (int)max(min(i64, (long long)1 << 30), -((long long)1 << 30));
@@ -1362,6 +1396,15 @@ int grid_ps_impl(const NggGridArgs *a, int64_t c_off, int64_t c_stride, const Ng
             pa.c_stride = c_stride; pa.c_off = c_off;
             pa.nu = nu; pa.nv = nv;
             pa.nk = nk; pa.p0 = (int)p0; pa.os = a->oversampling;
+            {
+                const int64_t ku = (2 * (nu / 2) + 1) * (int64_t)a->oversampling;
+                const int64_t kv = (2 * (nv / 2) + 1) * (int64_t)a->oversampling;
+                pa.half_ok = a->oversampling >= 1 && ku < (1 << 24) && kv < (1 << 24);
+                pa.ku = (float)ku;
+                pa.kv = (float)kv;
+                pa.inv_os = 1.0f / (float)(a->oversampling >= 1 ? a->oversampling : 1);
+                pa.margin0 = 2e-8f * (float)a->oversampling + 2e-7f;
+            }
             pa.density = fused_w ? iw->density : nullptr;
             pa.factors = fused_w ? iw->factors : nullptr;
             pa.dchan = dchan;

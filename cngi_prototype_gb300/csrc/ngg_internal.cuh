@@ -139,6 +139,46 @@ __device__ __forceinline__ bool cell_pair(float xh, float xl, float sh, float sl
     return true;
 }
 
+// The same chain with one certified floor instead of two (gridding, where
+// os >= 1). With G = (u_pos + 0.5) * os the cell is floor(G / os) (=
+// trunc(u_pos + 0.5) for u_pos >= 0) and the offset is
+//     floor((idx - u_pos) * os + 0.5) = idx * os + floor((os + 1) / 2 - G),
+// and both change value only where 2G crosses an integer. So one pair
+// estimate of 2G = x * (2 os s) + (2 C + 1) os, certified to lie farther from
+// every integer than the margins of cell_pair (scaled to 2G: 1e-8 cells is
+// 2e-8 os, 1e-8 os + 1e-7 offset units is twice that) plus its own error
+// bound (3e-14 |2G|), gives both results: with H = floor(2G),
+//     idx = floor(floor(H / 2) / os),  off = idx * os + floor((os - H) / 2).
+// (s2h, s2l) = 2 os s as a pair (scale_pair), K = (2 C + 1) os < 2^24 exactly,
+// margin0 = 2e-8 os + 2e-7. Returns false unless 1 <= 2G < 2^24 and the
+// estimate is certified (the caller then uses cell_pair).
+__device__ __forceinline__ bool cell_half(float xh, float xl, float s2h, float s2l, float K, int os, float inv_os,
+                                          float margin0, int &idx, int &off) {
+    const float ph = __fmul_rn(xh, s2h);
+    const float pe = fmaf(xh, s2h, -ph);
+    const float pl = fmaf(xh, s2l, fmaf(xl, s2h, pe));
+    float th, te;
+    two_sum(ph, K, th, te);
+    const float tl = __fadd_rn(te, pl);
+    if (!(th >= 1.0f && th < 16777216.0f)) return false;   // also NaN
+    int h;
+    float fa, fb;
+    if (!floor_pair(th, tl, fmaf(3e-14f, th, margin0), h, fa, fb)) return false;
+    const int gi = h >> 1;
+    int q = __float2int_rz(__fmul_rn(__int2float_rn(gi), inv_os));   // within 1 of gi / os
+    const int r = gi - q * os;
+    q += r < 0 ? -1 : (r >= os ? 1 : 0);
+    idx = q;
+    off = q * os + ((os - h) >> 1);
+    return true;
+}
+
+// (h, l) ~ (sh + sl) * f for a small integer f (error ~2^-47 relative)
+__device__ __forceinline__ void scale_pair(float sh, float sl, float f, float &h, float &l) {
+    h = __fmul_rn(sh, f);
+    l = fmaf(sl, f, fmaf(sh, f, -h));
+}
+
 // The FP64 chain, operation for operation (used near rounding boundaries).
 static __device__ __noinline__ void cell_fp64(double x, double s, bool neg, int center, int os, long long &idx,
                                        long long &off) {

@@ -140,9 +140,11 @@ struct PackArgs {
     const unsigned char *flag;   // (T,B,c_stride,P), nonzero = flagged visibility (DATA mode), or NULL
     int64_t dnu, dnv, n_img;
     int continuum;
-    // cell_half's constants: K = (2 C + 1) os per axis, 1 / os, its margin;
-    // half_ok = 0 where K >= 2^24 (then cell_pair serves every step)
-    float ku, kv, inv_os, margin0;
+    // cell_half's constants: K = (2 C + 1) os per axis, ceil(2^40 / os), the
+    // margin; half_ok = 0 where K >= 2^24 (then cell_pair serves every step)
+    int ku, kv;
+    unsigned long long osm;
+    float margin0;
     int half_ok;
 };
 
@@ -262,9 +264,9 @@ __global__ void __launch_bounds__(256, 4) k_pack(const PackArgs a) {
         const float4 us = us4[i];
         if (c_ok && t < a.T && !isnan(us.x) && !isnan(us.z)) {
             int cu, ou, cv, ov;
-            if (!(a.half_ok && cell_half(us.x, us.y, s2uh, s2ul, a.ku, a.os, a.inv_os, a.margin0, cu, ou)))
+            if (!(a.half_ok && cell_half(us.x, us.y, s2uh, s2ul, a.ku, a.os, a.osm, a.margin0, cu, ou)))
                 cell_slow(us.x, us.y, a.chan + c, 0, a.uvw + (t * a.B + b) * 3, cu_c, a.os, cu, ou);
-            if (!(a.half_ok && cell_half(us.z, us.w, s2vh, s2vl, a.kv, a.os, a.inv_os, a.margin0, cv, ov)))
+            if (!(a.half_ok && cell_half(us.z, us.w, s2vh, s2vl, a.kv, a.os, a.osm, a.margin0, cv, ov)))
                 cell_slow(us.z, us.w, a.chan + c, 1, a.uvw + (t * a.B + b) * 3, cv_c, a.os, cv, ov);
             if (cu - SC >= 0 && cu + SC < a.nu && cv - SC >= 0 && cv + SC < a.nv) {
                 const int64_t base = ((t * a.B + b) * a.c_stride + a.c_off + c) * a.P + a.p0;
@@ -660,9 +662,9 @@ __device__ __noinline__ bool zero_next(const ZeroRows &z) {
 //    (both pols) and the 7 v taps, plus the step's cell: class c holds the
 //    tap whose cell has class c, tap k = (c - (cu - 3)) mod 7;
 //  * consumer: the 49 footprint cells are owned in Romein's residue classes:
-//    lane (kappa, g), kappa = lane % 7 the u class (u mod 7), g = lane / 7
-//    (0..3), holds the cells of u class kappa and v classes 2g and 2g+1 in
-//    registers (lanes 28-31 hold none). Thanks to the class order a lane
+//    lane 4 kappa + g, kappa the u class (u mod 7) and g in 0..3, holds the
+//    cells of u class kappa and v classes 2g and 2g+1 in registers (lanes
+//    28-31 hold none). Thanks to the class order a lane
 //    reads the same record slots at every step -- one 16-byte load of its u
 //    product, one 8-byte load of its two v taps -- and adds them with four
 //    paired FMAs.
@@ -761,12 +763,15 @@ __global__ void __launch_bounds__((NWT + 1) * 32, 1) k_tiles(const TileArgs a) {
     const int64_t n_zero_items = (int64_t)a.n_img * NP * nrb;
     const int os = a.os;
 
-    // this lane's residue classes (consumer)
+    // this lane's residue classes (consumer): lane = 4 kappa + g. A half-warp
+    // then reads at most 4 distinct u products (4 of the 7 16-byte slots of a
+    // step), which a 16-byte shared load serves in one wavefront per half-warp
+    // instead of two
     const bool act = lane < 28;
-    const int kap = lane % 7, g = lane / 7;
+    const int kap = act ? lane >> 2 : 6, g = lane & 3;   // lanes 28-31 read valid slots (and never flush)
     const int rho0 = 2 * g, rho1 = 2 * g + 1;
     const bool has1 = act && g < 3;
-    const int gr = g < 3 ? g : 3;   // lanes 28-31 read a valid slot (and never flush)
+    const int gr = g;
 
     // Warp NWT zeroes the rows outside the busy box: each of its lanes takes
     // blocks of rows from a counter and zeroes them with TMA bulk stores from
@@ -866,6 +871,7 @@ __global__ void __launch_bounds__((NWT + 1) * 32, 1) k_tiles(const TileArgs a) {
             const float4 *cA = recA + kap;                                      // this lane's slots
             const float2 *cT = reinterpret_cast<const float2 *>(recT) + gr;
             int jl = 0;
+            unsigned carry = NO_CELL;   // the warp's current cell: the last cell of its previous chunks
             for (int64_t j = rs; j < re; ++j) {
                 const uint2 m = m_nx;
                 const float4 d = d_nx;
@@ -909,18 +915,21 @@ __global__ void __launch_bounds__((NWT + 1) * 32, 1) k_tiles(const TileArgs a) {
                         rt[1] = make_float4(0.f, 0.f, 0.f, 0.f);
                     }
                     recC[lane] = m.x;
-                    // a step whose cell differs from the cell of the chunk's last step
-                    // before it that has one (steps without a cell add zeros to whatever
-                    // cells are current, so they do not end a run; the chunk's first step
-                    // with a cell is marked as well, a no-op when its cell is current)
+                    // a step whose cell differs from the cell of the latest step before it
+                    // that has one (steps without a cell add zeros to whatever cells are
+                    // current, so they do not end a run; the cells are absolute, so the
+                    // previous chunk's last cell carries over even from another track)
                     unsigned last = m.x;   // the cell of this step or of the latest step before it that has one
 #pragma unroll
                     for (int o = 1; o < 32; o <<= 1) {
                         const unsigned t = __shfl_up_sync(0xffffffffu, last, o);
                         if (lane >= o && last == NO_CELL) last = t;
                     }
-                    const unsigned prev = __shfl_up_sync(0xffffffffu, last, 1);
-                    chg = __ballot_sync(0xffffffffu, m.x != NO_CELL && (lane == 0 || m.x != prev));
+                    unsigned prev = __shfl_up_sync(0xffffffffu, last, 1);
+                    if (lane == 0 || prev == NO_CELL) prev = carry;
+                    chg = __ballot_sync(0xffffffffu, m.x != NO_CELL && m.x != prev);
+                    const unsigned tail = __shfl_sync(0xffffffffu, last, 31);
+                    if (tail != NO_CELL) carry = tail;
                 }
                 __syncwarp();
                 // ---- consumer: the chunk's 32 steps, in runs between cell changes ----
@@ -1041,7 +1050,8 @@ int dispatch_tiles(const TileArgs &ta, int64_t n_bound, bool cplx, bool fftl, cu
 }
 
 __global__ void k_cell_indices(int64_t n_rows, int64_t C, const double *uvw, const double *freq, int64_t nu, int64_t nv,
-                               double dl0, double dl1, int os, int mirror, int32_t *idx, unsigned long long *nfb) {
+                               double dl0, double dl1, int os, int mirror, unsigned long long osm, float margin0,
+                               int32_t *idx, unsigned long long *nfb) {
     const int64_t id = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
     if (id >= n_rows * C) return;
     const int64_t r = id / C, c = id % C;
@@ -1058,10 +1068,10 @@ __global__ void k_cell_indices(int64_t n_rows, int64_t C, const double *uvw, con
     float s2uh, s2ul, s2vh, s2vl;
     scale_pair(a.hi, a.lo, os2, s2uh, s2ul);
     scale_pair(b.hi, b.lo, os2, s2vh, s2vl);
-    const bool half_ok = os >= 1 && (int64_t)(2 * cu_c + 1) * os < (1 << 24) && (int64_t)(2 * cv_c + 1) * os < (1 << 24);
-    const float Ku = (float)((2 * cu_c + 1) * os), Kv = (float)((2 * cv_c + 1) * os);
-    const float inv_os = 1.0f / (float)max(os, 1), margin0 = fmaf(2e-8f, (float)os, 2e-7f);
-    if (!(half_ok && cell_half(x.hi, x.lo, s2uh, s2ul, Ku, os, inv_os, margin0, cu, ou)) &&
+    const bool half_ok = os >= 1 && os < 65536 && (int64_t)(2 * cu_c + 1) * os < (1 << 24) &&
+                         (int64_t)(2 * cv_c + 1) * os < (1 << 24);
+    const int Ku = (2 * cu_c + 1) * os, Kv = (2 * cv_c + 1) * os;
+    if (!(half_ok && cell_half(x.hi, x.lo, s2uh, s2ul, Ku, os, osm, margin0, cu, ou)) &&
         !cell_pair(x.hi, x.lo, a.hi, a.lo, mirror != 0, cu_c, os, cu, ou)) {
         long long i64, o64;
         cell_fp64(u, su, mirror != 0, (int)(nu / 2), os, i64, o64);
@@ -1069,7 +1079,7 @@ __global__ void k_cell_indices(int64_t n_rows, int64_t C, const double *uvw, con
         ou = (int)max(min(o64, (long long)1 << 30), -((long long)1 << 30));
         ++fb;
     }
-    if (!(half_ok && cell_half(y.hi, y.lo, s2vh, s2vl, Kv, os, inv_os, margin0, cv, ov)) &&
+    if (!(half_ok && cell_half(y.hi, y.lo, s2vh, s2vl, Kv, os, osm, margin0, cv, ov)) &&
         !cell_pair(y.hi, y.lo, b.hi, b.lo, mirror != 0, cv_c, os, cv, ov)) {
         long long i64, o64;
         cell_fp64(v, sv, mirror != 0, (int)(nv / 2), os, i64, o64);
@@ -1399,11 +1409,11 @@ int grid_ps_impl(const NggGridArgs *a, int64_t c_off, int64_t c_stride, const Ng
             {
                 const int64_t ku = (2 * (nu / 2) + 1) * (int64_t)a->oversampling;
                 const int64_t kv = (2 * (nv / 2) + 1) * (int64_t)a->oversampling;
-                pa.half_ok = a->oversampling >= 1 && ku < (1 << 24) && kv < (1 << 24);
-                pa.ku = (float)ku;
-                pa.kv = (float)kv;
-                pa.inv_os = 1.0f / (float)(a->oversampling >= 1 ? a->oversampling : 1);
-                pa.margin0 = 2e-8f * (float)a->oversampling + 2e-7f;
+                pa.half_ok = a->oversampling >= 1 && a->oversampling < 65536 && ku < (1 << 24) && kv < (1 << 24);
+                pa.ku = (int)ku;
+                pa.kv = (int)kv;
+                pa.osm = os_magic(a->oversampling);
+                pa.margin0 = half_margin(a->oversampling);
             }
             pa.density = fused_w ? iw->density : nullptr;
             pa.factors = fused_w ? iw->factors : nullptr;
@@ -1464,7 +1474,8 @@ extern "C" int ngg_cell_indices(int64_t n_rows, int64_t C, const double *uvw, co
     if (!uvw || !freq || !idx) return fail(NGG_ERR_INVALID, "NULL pointer");
     const int64_t n = n_rows * C;
     k_cell_indices<<<(unsigned)((n + 255) / 256), 256, 0, s>>>(n_rows, C, uvw, freq, nu, nv, delta_lm[0], delta_lm[1],
-                                                               os, mirror, idx, (unsigned long long *)n_fallback);
+                                                               os, mirror, os_magic(os), half_margin(os), idx,
+                                                               (unsigned long long *)n_fallback);
     NGG_CHECK_LAUNCH("k_cell_indices");
     return NGG_OK;
 }

@@ -143,35 +143,42 @@ __device__ __forceinline__ bool cell_pair(float xh, float xl, float sh, float sl
 // os >= 1). With G = (u_pos + 0.5) * os the cell is floor(G / os) (=
 // trunc(u_pos + 0.5) for u_pos >= 0) and the offset is
 //     floor((idx - u_pos) * os + 0.5) = idx * os + floor((os + 1) / 2 - G),
-// and both change value only where 2G crosses an integer. So one pair
-// estimate of 2G = x * (2 os s) + (2 C + 1) os, certified to lie farther from
-// every integer than the margins of cell_pair (scaled to 2G: 1e-8 cells is
-// 2e-8 os, 1e-8 os + 1e-7 offset units is twice that) plus its own error
-// bound (3e-14 |2G|), gives both results: with H = floor(2G),
+// and both change value only where 2G crosses an integer. 2G = P + K with
+// P = x * (2 os s) and the integer K = (2 C + 1) os, so one pair estimate of
+// P, certified to lie farther from every integer than the margins of
+// cell_pair (scaled to 2G: 1e-8 cells is 2e-8 os, 1e-8 os + 1e-7 offset
+// units is twice that) plus its own error bound (3e-14 |P|), gives both
+// results: with H = K + floor(P),
 //     idx = floor(floor(H / 2) / os),  off = idx * os + floor((os - H) / 2).
-// (s2h, s2l) = 2 os s as a pair (scale_pair), K = (2 C + 1) os < 2^24 exactly,
-// margin0 = 2e-8 os + 2e-7. Returns false unless 1 <= 2G < 2^24 and the
+// floor(P) = r - (d < 0) with r = rint(ph) and d = (ph - r) + pl, the
+// signed distance of P from r (ph - r is exact). (s2h, s2l) = 2 os s as a
+// pair (scale_pair); the division by os is a multiplication by
+// osm = ceil(2^40 / os), exact for H < 2^25 and os < 2^16. margin0 =
+// 2e-8 os + 2e-7. Returns false unless |ph| < 2^24, 1 <= H < 2^24 and the
 // estimate is certified (the caller then uses cell_pair).
-__device__ __forceinline__ bool cell_half(float xh, float xl, float s2h, float s2l, float K, int os, float inv_os,
-                                          float margin0, int &idx, int &off) {
+__device__ __forceinline__ bool cell_half(float xh, float xl, float s2h, float s2l, int K, int os,
+                                          unsigned long long osm, float margin0, int &idx, int &off) {
     const float ph = __fmul_rn(xh, s2h);
     const float pe = fmaf(xh, s2h, -ph);
     const float pl = fmaf(xh, s2l, fmaf(xl, s2h, pe));
-    float th, te;
-    two_sum(ph, K, th, te);
-    const float tl = __fadd_rn(te, pl);
-    if (!(th >= 1.0f && th < 16777216.0f)) return false;   // also NaN
-    int h;
-    float fa, fb;
-    if (!floor_pair(th, tl, fmaf(3e-14f, th, margin0), h, fa, fb)) return false;
-    const int gi = h >> 1;
-    int q = __float2int_rz(__fmul_rn(__int2float_rn(gi), inv_os));   // within 1 of gi / os
-    const int r = gi - q * os;
-    q += r < 0 ? -1 : (r >= os ? 1 : 0);
+    if (!(fabsf(ph) < 16777216.0f)) return false;   // also NaN
+    const float r = rintf(ph);
+    const float d = __fadd_rn(__fsub_rn(ph, r), pl);
+    if (!(fabsf(d) > fmaf(3e-14f, fabsf(ph), margin0))) return false;
+    const int h = K + (int)r - (d < 0.0f ? 1 : 0);
+    if (h < 1 || h >= (1 << 24)) return false;
+    const int q = (int)(((unsigned long long)(unsigned)(h >> 1) * osm) >> 40);
     idx = q;
     off = q * os + ((os - h) >> 1);
     return true;
 }
+
+// cell_half's host-side constants: ceil(2^40 / os), so that floor(g / os) =
+// (g * os_magic(os)) >> 40 for g < 2^24 and 1 <= os < 2^16; and its margin
+inline unsigned long long os_magic(int os) {
+    return os >= 1 ? ((1ull << 40) + (unsigned long long)os - 1) / (unsigned long long)os : 0ull;
+}
+inline float half_margin(int os) { return 2e-8f * (float)os + 2e-7f; }
 
 // (h, l) ~ (sh + sl) * f for a small integer f (error ~2^-47 relative)
 __device__ __forceinline__ void scale_pair(float sh, float sl, float f, float &h, float &l) {

@@ -46,6 +46,9 @@ def parse():
     p.add_argument('--impl', default='ngg', choices=['ngg', 'reference'])
     p.add_argument('--n-time', type=int, default=1024)
     p.add_argument('--n-chan', type=int, default=256)
+    p.add_argument('--image-size', type=int, default=4096,
+                   help='large_cube: image side in pixels, cell 4096/N arcsec (the same field); smaller sizes are '
+                        'profiling cases of the same kernels, not the headline workload')
     p.add_argument('--cpu-chans', type=int, default=16, help='channels in the CPU-baseline sample')
     p.add_argument('--no-e2e', action='store_true')
     p.add_argument('--no-cpu', action='store_true')
@@ -143,11 +146,16 @@ def oracle_sample(uvw, vis_s, w_s, freq_s, cgk, npad, cell, threads):
     return g, sw, dt
 
 
-def large_cube_config(T, B, C, P, world):
+def large_cube_config(T, B, C, P, world, image_size=4096):
     """The `config` of the large-cube line (both arms)."""
+    from cngi_prototype_gb300.imaging._imaging_utils._check_imaging_parms import _check_grid_parms
+    gp = {'image_size': [image_size, image_size], 'cell_size': [4096.0 / image_size] * 2}
+    _check_grid_parms(gp)
     return {'workload': WORKLOAD, 'n_time': T, 'n_baseline': B, 'n_chan': C, 'n_pol': P, 'n_vis': T * B * C * P,
-            'image_size': 4096, 'grid': 4915, 'cell_arcsec': 1.0, 'weighting': 'briggs 0.5', 'support': 7,
-            'oversampling': 100, 'flags': 0.05, 'l2': 'inputs (12.7 GB) larger than L2; no flush',
+            'image_size': image_size, 'grid': int(gp['image_size_padded'][0]), 'cell_arcsec': 4096.0 / image_size,
+            'weighting': 'briggs 0.5', 'support': 7,
+            'oversampling': 100, 'flags': 0.05,
+            'l2': f'inputs ({T * B * C * P * 12 / 1e9:.1f} GB) larger than L2; no flush',
             'parallelism': f'channel shard x{world} (no exchange)'}
 
 
@@ -156,6 +164,7 @@ def large_cube_obs(args, rank, world, device):
     [r*n_chan, (r+1)*n_chan) of one N*n_chan-channel cube)."""
     from cngi_prototype_gb300 import simulate
     return simulate.config_large_cube(seed=2, n_time=args.n_time, n_chan=args.n_chan * world, vis_device=device,
+                                      image_size=args.image_size,
                                       chan_range=(rank * args.n_chan, (rank + 1) * args.n_chan))
 
 
@@ -206,7 +215,7 @@ def reference_arm(args, rank):
         'impl': 'reference', 'metric': METRIC, 'value': v, 'unit': 'Mvis/s', 'n_gpus': args.gpus,
         'steps': args.steps, 'warmup': args.warmup, 'ms_per_step': float(np.mean(times)) * 1e3,
         'higher_is_better': True, 'scaling': 'weak', 'vs_baseline': None, 'dtype': 'f64', 'data': 'synthetic',
-        'config': large_cube_config(T, B, C, P, 1),
+        'config': large_cube_config(T, B, C, P, 1, args.image_size),
         'cpu_baseline': {'value': v, 'unit': 'Mvis/s', 'cores': threads, 'kind': 'port',
                          'sample': f'channels 0-{nc - 1} of the {C}-channel cube (same seed, flags and Briggs 0.5 '
                                    f'weights as the GPU arm): all {T}x{B} rows x {P} pols ({nvis} vis) per step, C '
@@ -1157,7 +1166,7 @@ def main():
             'metric': METRIC, 'value': value, 'unit': 'Mvis/s', 'n_gpus': world, 'steps': args.steps,
             'warmup': args.warmup, 'ms_per_step': ms, 'higher_is_better': True, 'scaling': 'weak',
             'vs_baseline': None, 'dtype': 'f32', 'data': 'synthetic',
-            'config': large_cube_config(T, B, C, P, world),
+            'config': large_cube_config(T, B, C, P, world, args.image_size),
             'roofline': roofline, 'cpu_baseline': cpu, 'e2e': e2e, 'err_vs_fp64': err, 'clocks': clk,
             'gpu_launches': 11 * args.steps, 'mosaic': mosaic,
         }

@@ -234,18 +234,21 @@ def config_standard_small(seed=1, n_time=600, n_chan=32):
                             np.deg2rad(0.5), 0.1, (512, 512), (2.0, 2.0), seed)
 
 
-def config_large_cube(seed=2, n_time=1024, n_chan=256, vis_device=None, with_vis=True, chan_range=None):
+def config_large_cube(seed=2, n_time=1024, n_chan=256, vis_device=None, with_vis=True, chan_range=None,
+                      image_size=4096):
     """Large cube: 64 antennas, 3-arm log spiral of 2.5 km radius, 1024 x 8 s,
     256 channels over 1.0-1.5 GHz, RR/LL, 200 power-law sources
     (1 mJy-1 Jy), 5% random flags, Briggs 0.5, 4096^2 image at 1 arcsec.
     chan_range=(c0, c1) keeps channels c0..c1-1 of the n_chan (one rank's
-    shard of a channel-partitioned cube; same sky and rows)."""
+    shard of a channel-partitioned cube; same sky and rows). image_size N
+    images the same field with N^2 pixels of 4096/N arcsec."""
     freq = 1.0e9 + (np.arange(n_chan) + 0.5) * (0.5e9 / n_chan)
     if chan_range is not None:
         freq = freq[chan_range[0]:chan_range[1]]
     fov = 4096 * np.deg2rad(1.0 / 3600) / 2
+    cell = 4096.0 / image_size
     return make_observation(64, 'log_spiral', 2500.0, n_time, 8.0, freq, 2, 200, (1e-3, 1.0),
-                            fov, 0.05, (4096, 4096), (1.0, 1.0), seed, flag_fraction=0.05,
+                            fov, 0.05, (image_size, image_size), (cell, cell), seed, flag_fraction=0.05,
                             flux_law='power', vis_device=vis_device, with_vis=with_vis)
 
 

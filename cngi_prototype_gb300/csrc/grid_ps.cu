@@ -146,6 +146,9 @@ struct PackArgs {
     unsigned long long osm;
     float margin0;
     int half_ok;
+    // both pols of a step load as one 16-byte visibility and one 8-byte
+    // weight access (2 pols from pol 0, aligned buffers)
+    int vec2;
 };
 
 // cell_pair, then the FP64 chain: the packing pass's rare path (a step near a
@@ -248,10 +251,23 @@ __global__ void __launch_bounds__(256, 4) k_pack(const PackArgs a) {
         if (c_ok && t < a.T) {
             us4[i] = a.uvs[b * a.T + t];
             const int64_t base = ((t * a.B + b) * a.c_stride + a.c_off + c) * a.P + a.p0;
+            if (NP == 2 && a.vec2) {   // both pols of a (time, baseline, channel) in one 16- and one 8-byte load
+                if (!FUSED) {
+                    const float2 w2 = *reinterpret_cast<const float2 *>(a.weight + base);
+                    wl[i][0] = w2.x;
+                    wl[i][NP - 1] = w2.y;
+                }
+                if constexpr (CPLX) {
+                    const float4 v4 = *reinterpret_cast<const float4 *>(a.vis + base);
+                    vl[i][0] = make_float2(v4.x, v4.y);
+                    vl[i][NP - 1] = make_float2(v4.z, v4.w);
+                }
+            } else {
 #pragma unroll
-            for (int p = 0; p < NP; ++p) {
-                if (!FUSED) wl[i][p] = a.weight[base + p];
-                if constexpr (CPLX) vl[i][p] = a.vis[base + p];
+                for (int p = 0; p < NP; ++p) {
+                    if (!FUSED) wl[i][p] = a.weight[base + p];
+                    if constexpr (CPLX) vl[i][p] = a.vis[base + p];
+                }
             }
         }
     }
@@ -1414,6 +1430,8 @@ int grid_ps_impl(const NggGridArgs *a, int64_t c_off, int64_t c_stride, const Ng
                 pa.kv = (int)kv;
                 pa.osm = os_magic(a->oversampling);
                 pa.margin0 = half_margin(a->oversampling);
+                pa.vec2 = np == 2 && P == 2 && p0 == 0 && ((uintptr_t)vis_d & 15) == 0 &&
+                          ((uintptr_t)weight_d & 7) == 0;
             }
             pa.density = fused_w ? iw->density : nullptr;
             pa.factors = fused_w ? iw->factors : nullptr;

@@ -63,6 +63,8 @@ def parse():
     p.add_argument('--mosaic-pointings', type=int, default=49)
     p.add_argument('--no-learned', action='store_true')
     p.add_argument('--no-mosaic', action='store_true', help='large_cube: skip the mosaic (table vs learned GCF) record')
+    p.add_argument('--no-others', action='store_true',
+                   help='large_cube: skip the small-cube and degrid/grid records')
     p.add_argument('--learned-steps', type=int, default=30000)
     p.add_argument('--learned-freqs', type=int, default=64)
     return p.parse_args()
@@ -350,7 +352,9 @@ def _timed(fn, steps, warmup):
     return e0.elapsed_time(e1) / steps
 
 
-def _line(args, world, workload, value, ms, config, roofline, cpu, e2e, err, clk, launches, extra=None):
+def _line(args, world, workload, value, ms, config, roofline, cpu, e2e, err, clk, launches, extra=None, emit=True):
+    """A workload's JSON line: printed when the workload runs on its own,
+    returned for the records the large-cube line carries."""
     line = {'metric': METRIC, 'value': value, 'unit': 'Mvis/s', 'n_gpus': world, 'steps': args.steps,
             'warmup': args.warmup, 'ms_per_step': ms, 'higher_is_better': True, 'scaling': 'weak',
             'vs_baseline': None, 'dtype': 'f32', 'data': 'synthetic', 'config': {'workload': workload, **config},
@@ -358,10 +362,12 @@ def _line(args, world, workload, value, ms, config, roofline, cpu, e2e, err, clk
             'gpu_launches': launches}
     if extra:
         line.update(extra)
-    print(json.dumps(line), flush=True)
+    if emit:
+        print(json.dumps(line), flush=True)
+    return line
 
 
-def run_standard_small(args, rank, world, local, dist):
+def run_standard_small(args, rank, world, local, dist, emit=True):
     """The small standard cube (27 antennas, 600 x 10 s, 32 channels, RR/LL,
     512^2 at 2 arcsec, natural weighting): ngg_grid_ps device-resident, and
     make_imaging_weight + make_psf + make_image end to end from host arrays."""
@@ -447,14 +453,14 @@ def run_standard_small(args, rank, world, local, dist):
                          'at this size) vs the FP64 oracle grid + numpy FFT; gridding_image_max: ngg_grid_ps grid '
                          '+ numpy FP64 FFT; image_max_fft32: make_image with fft_precision single'}
     if rank == 0:
-        _line(args, world, 'standard_small_natural', value, ms,
+        return _line(args, world, 'standard_small_natural', value, ms,
               {'n_time': T, 'n_baseline': B, 'n_chan': C, 'n_pol': P, 'n_vis': n_vis, 'image_size': 512,
                'grid': int(npad[0]), 'cell_arcsec': 2.0, 'weighting': 'natural', 'support': 7, 'oversampling': 100,
                'l2': 'grid and inputs (0.5 GB) larger than L2', 'parallelism': f'replica x{world}'},
-              roofline, cpu, e2e, err, None, 11 * args.steps)
+              roofline, cpu, e2e, err, None, 11 * args.steps, emit=emit)
 
 
-def run_degrid(args, rank, world, local, dist):
+def run_degrid(args, rank, world, local, dist, emit=True):
     """Differentiable degrid/grid pair: 2048^2 float32 model of 500 Gaussian
     blobs (FWHM 2-20 px), 64 antennas x 992 times (2.0M rows), 64 channels
     over 1.0-1.5 GHz, 1 pol, 1 arcsec cells. One step = model visibilities
@@ -513,13 +519,14 @@ def run_degrid(args, rank, world, local, dist):
                'sample': f'the gradient half (gridding) of channels 0-{nc - 1}: C FP64 restatement of '
                          f'_standard_grid_jit; the reference has no degridder'}
     if rank == 0:
-        _line(args, world, 'degrid_grid_chi2_step', value, ms,
+        return _line(args, world, 'degrid_grid_chi2_step', value, ms,
               {'n_time': T, 'n_baseline': B, 'n_chan': C, 'n_pol': P, 'n_vis': n_vis, 'image_size': N,
                'grid': int(op.npad[0]), 'cell_arcsec': 1.0, 'model': '500 Gaussians, FWHM 2-20 px',
                'parallelism': f'replica x{world}'},
               None, cpu, None, None, None, 12 * args.steps,
               {'forward_degrid_ms': fwd_ms, 'backward_grid_ms': bwd_ms,
-               'note': 'value = model visibilities per second of one forward + chi-square + backward step'})
+               'note': 'value = model visibilities per second of one forward + chi-square + backward step'},
+              emit=emit)
 
 
 def _ev_ms(fn, steps, warmup):
@@ -1153,13 +1160,25 @@ def main():
 
     # ---- the metric's second half: learned vs table GCF mosaic imaging ----
     mosaic = None
-    if not args.no_mosaic:
+    if not (args.no_mosaic and args.no_others):   # the large cube's device arrays are no longer needed
         del vis_d, w_d, iw_d, sw, uvw_d, freq_d, cgk_d, obs
         grid = None   # (already released by the end-to-end leg when it ran)
         torch.cuda.empty_cache()
+    if not args.no_mosaic:
         mrec = mosaic_measure(args, rank, world, local, dist, with_e2e=False, with_cpu=False,
                               steps=min(args.steps, 10), warmup=3)
         mosaic = mosaic_summary(mrec)
+
+    # ---- the other single-GPU configurations: small cube, degrid/grid pair ----
+    others = None
+    if not args.no_others:
+        others = {}
+        for key, fn in (('standard_small', run_standard_small), ('degrid', run_degrid)):
+            rec = fn(args, rank, world, local, dist, emit=False)
+            if rank == 0:
+                others[key] = {k: rec.get(k) for k in ('config', 'value', 'unit', 'ms_per_step', 'roofline',
+                                                          'cpu_baseline', 'e2e', 'err_vs_fp64', 'forward_degrid_ms',
+                                                          'backward_grid_ms', 'note') if rec.get(k) is not None}
 
     if rank == 0:
         line = {
@@ -1168,7 +1187,7 @@ def main():
             'vs_baseline': None, 'dtype': 'f32', 'data': 'synthetic',
             'config': large_cube_config(T, B, C, P, world, args.image_size),
             'roofline': roofline, 'cpu_baseline': cpu, 'e2e': e2e, 'err_vs_fp64': err, 'clocks': clk,
-            'gpu_launches': 11 * args.steps, 'mosaic': mosaic,
+            'gpu_launches': 11 * args.steps, 'mosaic': mosaic, 'other_configs': others,
         }
         print(json.dumps(line), flush=True)
     if dist:

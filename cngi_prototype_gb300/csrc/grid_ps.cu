@@ -215,13 +215,13 @@ __global__ void __launch_bounds__(256, 4) k_pack(const PackArgs a) {
     __shared__ float4 s_wv[32][33];
     __shared__ float s_sw[NP][32][9];       // per channel: the 8 row-threads' partial sums
     __shared__ float s_nsum[MAX_OS + 1];
+    __shared__ float4 s_uvs[CH];             // the chunk's uvw pairs (every channel lane shares them)
     const int x = threadIdx.x;
     const int64_t b = blockIdx.x;
     const int k = blockIdx.y;
     const int64_t c0 = (int64_t)blockIdx.z * 32;
     const int cu_c = (int)(a.nu / 2), cv_c = (int)(a.nv / 2);
     for (int i = threadIdx.y * 32 + x; i <= a.os; i += 256) s_nsum[i] = a.nsum[i];
-    __syncthreads();
     float swc[NP];   // this thread's sum_weight terms over its 4 steps
 #pragma unroll
     for (int p = 0; p < NP; ++p) swc[p] = 0.f;
@@ -236,20 +236,17 @@ __global__ void __launch_bounds__(256, 4) k_pack(const PackArgs a) {
     float s2uh, s2ul, s2vh, s2vl;
     scale_pair(cp.suh, cp.sul, (float)(2 * a.os), s2uh, s2ul);
     scale_pair(cp.svh, cp.svl, (float)(2 * a.os), s2vh, s2vl);
-    float4 us4[4];
     float wl[4][NP];
     float2 vl[4][NP];
 #pragma unroll
     for (int i = 0; i < 4; ++i) {
         const int64_t t = (int64_t)k * CH + threadIdx.y + 8 * i;
-        us4[i] = make_float4(NAN, 0.f, NAN, 0.f);
 #pragma unroll
         for (int p = 0; p < NP; ++p) {
             wl[i][p] = 0.f;
             vl[i][p] = make_float2(0.f, 0.f);
         }
         if (c_ok && t < a.T) {
-            us4[i] = a.uvs[b * a.T + t];
             const int64_t base = ((t * a.B + b) * a.c_stride + a.c_off + c) * a.P + a.p0;
             if (NP == 2 && a.vec2) {   // both pols of a (time, baseline, channel) in one 16- and one 8-byte load
                 if (!FUSED) {
@@ -271,13 +268,20 @@ __global__ void __launch_bounds__(256, 4) k_pack(const PackArgs a) {
             }
         }
     }
+    // the uvw pairs through shared memory (issued after the visibility and
+    // weight loads, so that all of them are in flight together)
+    if (threadIdx.y == 0) {
+        const int64_t t = (int64_t)k * CH + x;
+        s_uvs[x] = t < a.T ? a.uvs[b * a.T + t] : make_float4(NAN, 0.f, NAN, 0.f);
+    }
+    __syncthreads();
 #pragma unroll
     for (int i = 0; i < 4; ++i) {
         const int y = threadIdx.y + 8 * i;
         const int64_t t = (int64_t)k * CH + y;
         uint2 meta = make_uint2(NO_CELL, 0u);
         float4 wv = make_float4(0.f, 0.f, 0.f, 0.f);
-        const float4 us = us4[i];
+        const float4 us = s_uvs[y];
         if (c_ok && t < a.T && !isnan(us.x) && !isnan(us.z)) {
             int cu, ou, cv, ov;
             if (!(a.half_ok && cell_half(us.x, us.y, s2uh, s2ul, a.ku, a.os, a.osm, a.margin0, cu, ou)))

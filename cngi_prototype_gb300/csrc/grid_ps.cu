@@ -455,12 +455,12 @@ __global__ void k_emit(const float4 *bbox, const ChanParms *chan, int64_t C, int
     TileRange r = chunk_tiles(bbox[bk], chan[c], nu, nv, ntu, ntv);
     if (!(r.u0 <= r.u1 && r.v0 <= r.v1)) return;
     unsigned long long o = offsets[ch];
-    int64_t cimg = continuum ? 0 : c;
-    int64_t NT = (int64_t)ntu * ntv;
+    // the key is (tile, chunk): the chunk index is channel-major, so keys in
+    // tile order are in (tile, image channel) bin order as well
     for (int tu = r.u0; tu <= r.u1; ++tu)
         for (int tv = r.v0; tv <= r.v1; ++tv) {
-            unsigned long long bin = (unsigned long long)(cimg * NT + (int64_t)tu * ntv + tv);
-            keys[o++] = (bin << 32) | (unsigned long long)ch;
+            const unsigned long long tile = (unsigned long long)((int64_t)tu * ntv + tv);
+            keys[o++] = (tile << 32) | (unsigned long long)ch;
         }
 }
 
@@ -469,19 +469,24 @@ __global__ void k_bbox_init(int *bb) {
 }
 
 // range of tiles holding any chunk, over all image channels
-__global__ void k_bbox(const int64_t *bin_start, int64_t n_bins, int64_t NT, int ntv, int *bb) {
+__global__ void k_bbox(const int64_t *bin_start, int64_t n_bins, int n_img, int ntv, int *bb) {
     const int64_t bin = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
     if (bin >= n_bins || bin_start[bin] == bin_start[bin + 1]) return;
-    const int64_t tile = bin % NT;
+    const int64_t tile = bin / n_img;
     const int tu = (int)(tile / ntv), tv = (int)(tile % ntv);
     atomicMin(&bb[0], tu); atomicMax(&bb[1], tu);
     atomicMin(&bb[2], tv); atomicMax(&bb[3], tv);
 }
 
-__global__ void k_bounds(const unsigned long long *keys, int64_t n, int64_t n_bins, int64_t *bin_start) {
+// bin = tile * n_img + image channel; its first key is (tile, the image
+// channel's first chunk) (chunks_per_img = B * nk in cube mode, 0 in
+// continuum mode, where every channel is image channel 0)
+__global__ void k_bounds(const unsigned long long *keys, int64_t n, int64_t n_bins, int n_img,
+                         int64_t chunks_per_img, int64_t *bin_start) {
     int64_t bin = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
     if (bin > n_bins) return;
-    unsigned long long target = (unsigned long long)bin << 32;
+    const unsigned long long target = ((unsigned long long)(bin / n_img) << 32) |
+                                      (unsigned long long)((bin % n_img) * chunks_per_img);
     int64_t lo = 0, hi = n;
     while (lo < hi) {
         int64_t mid = (lo + hi) >> 1;
@@ -526,7 +531,7 @@ struct BoxMap {
         cimg = (int)(item % n_img);
         tiu = bt0 + (int)(tix / nbv);
         tiv = bv0 + (int)(tix % nbv);
-        bin = (int64_t)cimg * NT + (int64_t)tiu * ntv + tiv;
+        bin = ((int64_t)tiu * ntv + tiv) * n_img + cimg;   // tile-major bins
     }
 };
 
@@ -1312,10 +1317,11 @@ int grid_ps_impl(const NggGridArgs *a, int64_t c_off, int64_t c_stride, const Ng
                                        a->chan_mode == NGG_CHAN_CONTINUUM, offsets, keys);
             NGG_CHECK_LAUNCH("k_emit");
             // k_emit writes each chunk's keys in chunk order, so a stable
-            // sort on the bin bits alone (LSD radix sort is stable) leaves
-            // every bin's chunks in (chan, baseline, time) order
+            // sort on the tile bits alone (LSD radix sort is stable) leaves
+            // every tile's chunks in (chan, baseline, time) order: sorted by
+            // the whole key, bins (tile, image channel) in order
             int end_bit = 32;
-            while (end_bit < 64 && ((unsigned long long)n_bins >> (end_bit - 32)) > 0) ++end_bit;
+            while (end_bit < 64 && ((unsigned long long)((int64_t)ntu * ntv) >> (end_bit - 32)) > 0) ++end_bit;
             size_t sort_bytes = 0;
             NGG_CUDA(cub::DeviceRadixSort::SortKeys(nullptr, sort_bytes, keys, keys_sorted, n_keys, 32, end_bit, s));
             void *stmp = nullptr;
@@ -1323,7 +1329,8 @@ int grid_ps_impl(const NggGridArgs *a, int64_t c_off, int64_t c_stride, const Ng
             NGG_CUDA(cub::DeviceRadixSort::SortKeys(stmp, sort_bytes, keys, keys_sorted, n_keys, 32, end_bit, s));
         }
     }
-    k_bounds<<<(unsigned)((n_bins + 1 + 255) / 256), 256, 0, s>>>(keys_sorted, n_keys, n_bins, bin_start);
+    k_bounds<<<(unsigned)((n_bins + 1 + 255) / 256), 256, 0, s>>>(
+        keys_sorted, n_keys, n_bins, (int)n_img, a->chan_mode == NGG_CHAN_CONTINUUM ? 0 : B * (int64_t)nk, bin_start);
     NGG_CHECK_LAUNCH("k_bounds");
 
     int *counter = nullptr;
@@ -1332,7 +1339,7 @@ int grid_ps_impl(const NggGridArgs *a, int64_t c_off, int64_t c_stride, const Ng
     int *bbox_d = nullptr;
     if ((rc = sc.get((void **)&bbox_d, sizeof(int) * 4)) != NGG_OK) return rc;
     k_bbox_init<<<1, 1, 0, s>>>(bbox_d);
-    k_bbox<<<(unsigned)((n_bins + 255) / 256), 256, 0, s>>>(bin_start, n_bins, (int64_t)ntu * ntv, ntv, bbox_d);
+    k_bbox<<<(unsigned)((n_bins + 255) / 256), 256, 0, s>>>(bin_start, n_bins, (int)n_img, ntv, bbox_d);
     NGG_CHECK_LAUNCH("k_bbox");
     // tile work items: every (tile in the busy box, channel); bins with more
     // than MAXE entries become several items

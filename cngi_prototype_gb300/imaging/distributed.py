@@ -18,9 +18,12 @@ the visibilities, and the graph reduces to at most one sum per call:
   weighting first add up the weight-density grid (unpadded, N0*N1 per pol)
   and its weight sum, between the density pass and the lookup pass.
 
-The sums run over torch.distributed on host tensors (gloo over TCP): each
-box holds one GPU, nothing waits on the device, and no NCCL is involved. A
-rank that fails can mark itself in a store shared by the group
+The sums run over torch.distributed. With a gloo group they add host
+tensors (TCP between boxes of one GPU each; nothing waits on the device).
+With an NCCL group (the GPUs of one node) the weight-density grid, which is
+already on the device, is added on the device with no host copy; the
+continuum image is added on the host either way, since the API returns it
+as a host dataset. A rank that fails can mark itself in a store shared by the group
 (ShardGroup.fail); the others see the mark before their next sum
 (ShardGroup.check) instead of waiting out the process-group timeout, and
 every sum that does not complete raises ShardError.
@@ -110,9 +113,21 @@ class ShardGroup:
             if self.store.check([key]):
                 raise ShardError(f'rank {r} failed: {self.store.get(key).decode(errors="replace")}')
 
+    def _nccl(self):
+        if self.world == 1:
+            return False
+        try:
+            return str(self._dist.get_backend(self.group)).lower() == 'nccl'
+        except (RuntimeError, ValueError):
+            return False
+
     def sum(self, arrays):
         """Element-wise sum over the ranks of a list of arrays (numpy or torch,
-        any device); returns float64 numpy arrays of the same shapes."""
+        any device); returns float64 numpy arrays of the same shapes, or, in
+        an NCCL group when every array is a CUDA tensor, float64 CUDA tensors
+        (summed on the device)."""
+        if self._nccl() and all(getattr(a, 'is_cuda', False) for a in arrays):
+            return self._sum_device(arrays)
         vals = [np.asarray(a.detach().cpu().numpy() if hasattr(a, 'detach') else a, dtype=np.float64)
                 for a in arrays]
         self.check()
@@ -134,6 +149,27 @@ class ShardGroup:
         for v in vals:
             out.append(flat[k:k + v.size].reshape(v.shape).copy())
             k += v.size
+        return out
+
+    def _sum_device(self, arrays):
+        import torch
+        self.check()
+        flat = torch.cat([a.detach().reshape(-1).to(torch.float64) for a in arrays])
+        try:
+            work = self._dist.all_reduce(flat, op=self._dist.ReduceOp.SUM, group=self.group, async_op=True)
+            if self.timeout is not None:
+                work.wait(timeout=self.timeout)
+            else:
+                work.wait()
+            torch.cuda.current_stream(flat.device).synchronize()
+        except RuntimeError as e:
+            raise ShardError(f'sum over {self.world} ranks failed on rank {self.rank}: {e}') from e
+        self.check()
+        out, k = [], 0
+        for a in arrays:
+            n = a.numel()
+            out.append(flat[k:k + n].reshape(a.shape))
+            k += n
         return out
 
 

@@ -524,7 +524,6 @@ __device__ __forceinline__ bool mbar_wait(unsigned addr, unsigned phase) {
 // box item -> (tile index, image channel, bin)
 struct BoxMap {
     int bt0, bv0, nbu, nbv, n_img;
-    int64_t NT;
     int ntv;
     __device__ __forceinline__ void map(int64_t item, int &tiu, int &tiv, int &cimg, int64_t &bin) const {
         const int64_t tix = item / n_img;
@@ -535,7 +534,7 @@ struct BoxMap {
     }
 };
 
-__device__ __forceinline__ BoxMap box_map(const int *bbox, int n_img, int64_t NT, int ntv) {
+__device__ __forceinline__ BoxMap box_map(const int *bbox, int n_img, int ntv) {
     BoxMap m;
     const bool have = bbox[0] <= bbox[1] && bbox[2] <= bbox[3];
     m.bt0 = bbox[0];
@@ -543,17 +542,15 @@ __device__ __forceinline__ BoxMap box_map(const int *bbox, int n_img, int64_t NT
     m.nbu = have ? bbox[1] - bbox[0] + 1 : 0;
     m.nbv = have ? bbox[3] - bbox[2] + 1 : 0;
     m.n_img = n_img;
-    m.NT = NT;
     m.ntv = ntv;
     return m;
 }
 
 // number of work items of every box item (0 beyond the box)
-__global__ void k_nsub(const int64_t *bin_start, const int *bbox, int n_img, int64_t NT, int ntv, int64_t n_bound,
-                       int *nsub) {
+__global__ void k_nsub(const int64_t *bin_start, const int *bbox, int n_img, int ntv, int64_t n_bound, int *nsub) {
     const int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
     if (i > n_bound) return;
-    const BoxMap m = box_map(bbox, n_img, NT, ntv);
+    const BoxMap m = box_map(bbox, n_img, ntv);
     const int64_t n_box = (int64_t)m.nbu * m.nbv * n_img;
     int k = 0;
     if (i < n_box) {
@@ -578,9 +575,9 @@ __global__ void k_fill_subs(const int *nsub, const int *off, int64_t n_bound, Su
 // their partial tiles with atomics); grid-stride over the busy box's items
 // (a few of the ~10^6 bins are split: one block per bin was all launch cost)
 template <bool CPLX, bool FFTL>
-__global__ void k_zero_split(const int64_t *bin_start, const int *bbox, int n_img, int64_t NT, int ntv,
+__global__ void k_zero_split(const int64_t *bin_start, const int *bbox, int n_img, int ntv,
                              int64_t n_bound, void *grid, int64_t P, int p0, int np, int64_t nu, int64_t nv) {
-    const BoxMap m = box_map(bbox, n_img, NT, ntv);
+    const BoxMap m = box_map(bbox, n_img, ntv);
     const int64_t n_box = (int64_t)m.nbu * m.nbv * n_img;
     for (int64_t i = blockIdx.x; i < n_bound && i < n_box; i += gridDim.x) {
     int tiu, tiv, cimg;
@@ -776,10 +773,9 @@ __global__ void __launch_bounds__((NWT + 1) * 32, 1) k_tiles(const TileArgs a) {
     float *recT = reinterpret_cast<float *>(recA + CH * SUP);                           // [CH][RT] by v class
     unsigned *recC = reinterpret_cast<unsigned *>(recT + CH * RT);                      // [CH]
 
-    const int64_t NT = (int64_t)a.ntu * a.ntv;
     const int cu_c = (int)(a.nu / 2), cv_c = (int)(a.nv / 2);
     const int64_t plane = a.nu * a.nv;
-    const BoxMap bm = box_map(a.bbox, a.n_img, NT, a.ntv);
+    const BoxMap bm = box_map(a.bbox, a.n_img, a.ntv);
     const int R0 = bm.nbu ? bm.bt0 * TU : 0, R1 = bm.nbu ? min((bm.bt0 + bm.nbu) * TU, (int)a.nu) : 0;
     const int V0 = bm.nbv ? bm.bv0 * TV : 0, V1 = bm.nbv ? min((bm.bv0 + bm.nbv) * TV, (int)a.nv) : 0;
     const int64_t n_tile_items = *a.n_subs;
@@ -1057,8 +1053,7 @@ int launch_tiles(const TileArgs &ta, int64_t n_bound, cudaStream_t s) {
     if (per_sm < 1) return fail(NGG_ERR_UNSUPPORTED, "k_tiles does not fit on an SM");
     if (n_bound > 0) {
         const int64_t zb = n_bound < (int64_t)num_sms() * 16 ? n_bound : (int64_t)num_sms() * 16;
-        k_zero_split<CPLX, FFTL><<<(unsigned)zb, 256, 0, s>>>(ta.bin_start, ta.bbox, ta.n_img,
-                                                                    (int64_t)ta.ntu * ta.ntv, ta.ntv, n_bound,
+        k_zero_split<CPLX, FFTL><<<(unsigned)zb, 256, 0, s>>>(ta.bin_start, ta.bbox, ta.n_img, ta.ntv, n_bound,
                                                                     ta.grid, ta.P, ta.p0, NP, ta.nu, ta.nv);
         NGG_CHECK_LAUNCH("k_zero_split");
     }
@@ -1352,8 +1347,7 @@ int grid_ps_impl(const NggGridArgs *a, int64_t c_off, int64_t c_stride, const Ng
     const int64_t max_subs = n_bound + n_keys / MAXE + 2;
     if (max_subs >= ((int64_t)1 << 31)) return fail(NGG_ERR_UNSUPPORTED, "too many tile work items");
     if ((rc = sc.get((void **)&subs, sizeof(SubItem) * max_subs)) != NGG_OK) return rc;
-    k_nsub<<<(unsigned)((n_bound + 1 + 255) / 256), 256, 0, s>>>(bin_start, bbox_d, n_img, (int64_t)ntu * ntv, ntv,
-                                                                n_bound, nsub);
+    k_nsub<<<(unsigned)((n_bound + 1 + 255) / 256), 256, 0, s>>>(bin_start, bbox_d, n_img, ntv, n_bound, nsub);
     NGG_CHECK_LAUNCH("k_nsub");
     {
         size_t tb = 0;

@@ -126,8 +126,10 @@ typedef struct NggImagingWeights {
 } NggImagingWeights;
 int ngg_grid_ps_weighted(const NggGridArgs *args, const NggImagingWeights *iw, void *stream);
 
-/* Cell and oversampling-offset indices as every kernel above computes them
- * (the FP32-pair evaluation with FP64 fallback): for each uvw row r and
+/* Cell and oversampling-offset indices as the gridder's packing pass
+ * computes them (one certified FP32-pair floor of 2 (u_pos + 0.5) os, then
+ * the two-floor FP32-pair chain, then FP64 near rounding boundaries; every
+ * path gives the FP64 chain's integers): for each uvw row r and
  * channel c, idx[(r*n_chan + c)*4 + {0,1,2,3}] = (cu, cv, ou, ov), with
  * cu = int(u_pos + 0.5), ou = floor((cu - u_pos)*oversampling + 0.5) and
  * likewise for v (_standard_grid.py:299-324), mirrored (-u, -v) when

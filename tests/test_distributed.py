@@ -7,7 +7,8 @@ over all the data. Failure tests: a rank that marks itself failed and
 leaves, and a rank that leaves silently, both end the other rank's next
 sum with ShardError instead of a hang. The GPU test runs the same groups
 through the CUDA path (two processes on one GPU; nothing waits on the
-device, the sums are on the host).
+device, the sums are on the host), and a one-rank NCCL group exercises the
+device-side sum.
 """
 import os
 import socket
@@ -142,3 +143,27 @@ def test_two_ranks_match_one_process_gpu(ngg, tmp_path, chan_mode):
     two = _launch(str(tmp_path / 'w2'), chan_mode, 'gpu', 2)
     one = _launch(str(tmp_path / 'w1'), chan_mode, 'gpu', 1)
     _check_against_single(two, one, chan_mode, 1e-5)
+
+
+@pytest.mark.gpu
+def test_device_sum_in_an_nccl_group(tmp_path):
+    """ShardGroup's NCCL branch (the continuum density grid summed on the
+    device): flatten, all-reduce and split CUDA tensors. A one-rank group on
+    this GPU exercises the calls; the sum over one rank is the input."""
+    code = f'''
+import torch, torch.distributed as dist
+dist.init_process_group('nccl', init_method='tcp://127.0.0.1:{_free_port()}', rank=0, world_size=1)
+from cngi_prototype_gb300.imaging.distributed import ShardGroup
+g = ShardGroup()
+a = torch.arange(12., device='cuda').reshape(3, 4).float()
+b = torch.full((5,), 0.25, device='cuda', dtype=torch.float32)
+out = g._sum_device([a, b])
+assert all(o.is_cuda and o.dtype == torch.float64 for o in out)
+assert out[0].shape == a.shape and out[1].shape == b.shape
+assert torch.equal(out[0], a.double()) and torch.equal(out[1], b.double())
+dist.destroy_process_group()
+print('device sum ok')
+'''
+    env = dict(os.environ, PYTHONPATH=ROOT + os.pathsep + os.environ.get('PYTHONPATH', ''))
+    r = subprocess.run([sys.executable, '-c', code], env=env, capture_output=True, text=True, timeout=180)
+    assert r.returncode == 0 and 'device sum ok' in r.stdout, r.stdout[-2000:] + r.stderr[-2000:]
